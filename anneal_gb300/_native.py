@@ -1,0 +1,104 @@
+"""ctypes binding of libanneal_gb300.so (the C ABI in include/anneal_gb300.h).
+
+The library is the only compute path: importing this module fails loudly when the
+shared object is missing, and every call checks the returned status.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libanneal_gb300.so")
+
+ANL_OK = 0
+ANL_ERR_MAXITER = 1
+ANL_ERR_NONFINITE = 2
+ANL_ERR_BREAKDOWN = 3
+ANL_ERR_BADARG = 4
+ANL_ERR_CUDA = 5
+ANL_ERR_SINGULAR = 6
+ANL_ERR_NOMEM = 7
+ANL_ERR_STATE = 8
+ANL_FLAG_FP64 = 1
+
+STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "NONFINITE", 3: "BREAKDOWN", 4: "BADARG", 5: "CUDA",
+                6: "SINGULAR", 7: "NOMEM", 8: "STATE"}
+
+# Every symbol include/anneal_gb300.h declares; tests check the library exports them all.
+EXPORTS = [
+    "anl_version", "anl_last_error", "anl_ctx_create", "anl_ctx_destroy", "anl_set_domain",
+    "anl_free_mask", "anl_apply_K", "anl_solve", "anl_dot", "anl_element_energy",
+    "anl_sensitivity", "anl_stiffness_scale", "anl_filter_init", "anl_filter_fwd",
+    "anl_filter_bwd", "anl_physical", "anl_oc_update", "anl_design_stats",
+]
+
+
+class NativeError(RuntimeError):
+    """A non-zero status from the CUDA library."""
+
+    def __init__(self, status, func, msg):
+        super().__init__(f"{func} failed with {STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+D = ctypes.c_double
+I64 = ctypes.c_int64
+
+_SIGS = {
+    "anl_version": (I, []),
+    "anl_last_error": (ctypes.c_char_p, []),
+    "anl_ctx_create": (I, [ctypes.POINTER(P), I, I, I, D, D, I]),
+    "anl_ctx_destroy": (None, [P]),
+    "anl_set_domain": (I, [P, P, P, ctypes.POINTER(I64), P]),
+    "anl_free_mask": (I, [P, P, P]),
+    "anl_apply_K": (I, [P, P, P, P, P]),
+    "anl_solve": (I, [P, P, P, P, I, D, I, I, ctypes.POINTER(I), ctypes.POINTER(D), P]),
+    "anl_dot": (I, [P, P, P, ctypes.POINTER(D), P]),
+    "anl_element_energy": (I, [P, P, P, P]),
+    "anl_sensitivity": (I, [P, P, I, ctypes.POINTER(D), P, P, P, D, D, D, P, P, P]),
+    "anl_stiffness_scale": (I, [P, P, P, D, D, D, P, P]),
+    "anl_filter_init": (I, [P, D, P]),
+    "anl_filter_fwd": (I, [P, P, P, P]),
+    "anl_filter_bwd": (I, [P, P, P, P]),
+    "anl_physical": (I, [P, P, P, D, D, P, P, P]),
+    "anl_oc_update": (I, [P, P, P, P, P, P, D, D, D, D, P, ctypes.POINTER(I), ctypes.POINTER(D), P]),
+    "anl_design_stats": (I, [P, P, P, P, P, P, ctypes.POINTER(D), P]),
+}
+
+
+def lib_path():
+    return LIB_PATH
+
+
+def load():
+    """Load the library (once). Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.isfile(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build the CUDA library first "
+                          f"(python -m anneal_gb300.build)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error():
+    return load().anl_last_error().decode(errors="replace")
+
+
+def check(status, func):
+    if status != ANL_OK:
+        raise NativeError(status, func, last_error())
+    return status
+
+
+def call(name, *args):
+    return check(getattr(load(), name)(*args), name)

@@ -1,0 +1,90 @@
+// anl_ctx.cuh -- the solver context behind the opaque anl_ctx handle.
+#pragma once
+
+#include <vector>
+
+#include "anl_common.cuh"
+#include "anl_kernels.cuh"
+
+namespace anl {
+
+// One level of the voxel hierarchy. Level 0 is the user's grid; level l+1 halves every
+// element dimension (rounded up). Vectors are in the context's precision T.
+struct Level {
+    Dims d{};
+    float* E = nullptr;       // element scale (times h at level 0; children sum / 4 below)
+    uint8_t* eact = nullptr;  // element is (or covers) an active element
+    uint8_t* nmask = nullptr; // node mask bits
+    float* diag = nullptr;    // diagonal of K per node (the same for the 3 DOFs of a node)
+    void* x = nullptr;        // V-cycle iterate (level 0: z = M r)
+    void* xt = nullptr;       // Chebyshev double buffer
+    void* b = nullptr;        // right-hand side (level 0: the CG residual r)
+    void* r = nullptr;        // residual scratch
+    void* dv = nullptr;       // Chebyshev direction
+    double lmax = 0.0;        // largest eigenvalue estimate of D^-1 K
+};
+
+struct FilterState {
+    bool ready = false;
+    int R = 0;
+    double r = 0.0;
+    float* w = nullptr;   // (2R+1)^3 cone weights, device
+    float* Hs = nullptr;  // conv(active), zeros replaced by 1
+};
+
+constexpr int kMaxFilterR = 5;
+
+}  // namespace anl
+
+struct anl_ctx {
+    anl::Dims d{};
+    double h = 1.0, nu = 0.3;
+    int flags = 0;
+    bool fp64 = false;
+    size_t tsize = 4;  // bytes per vector entry
+
+    double ke[576];                 // Ke(1) row-major (host)
+    double* ke_d = nullptr;         // Ke(1) on the device (coarse assembly)
+    anl::KeBlocks<double> kbd{};
+    anl::KeBlocks<float> kbf{};
+    double kdiag = 0.0;
+
+    bool domain_set = false;
+    int64_t nfree = 0;
+    uint8_t* active = nullptr;      // level-0 active flags (ne)
+    std::vector<anl::Level> lev;
+    int mg_degree = 2;
+
+    // coarsest level: dense factor (FP64) or a Chebyshev fallback when too large
+    int nc = 0;
+    bool dense_coarse = false;
+    bool coarse_ready = false;
+    double* A = nullptr;     // nc x nc, lower Cholesky factor after setup
+    double* Ainv = nullptr;  // nc x nc inverse
+    int* flag_d = nullptr;
+
+    // CG vectors (precision T) and FP64 solution / right-hand side
+    void* p = nullptr;
+    void* q = nullptr;
+    void* xhi = nullptr;
+    void* xlo = nullptr;
+    void* y1 = nullptr;
+    void* y2 = nullptr;
+    void* tmp = nullptr;
+    double* xbuf = nullptr;
+    double* bbuf = nullptr;
+
+    anl::PcgScalars* sc = nullptr;    // device
+    anl::PcgScalars* sc_h = nullptr;  // pinned host mirror
+
+    // reduction scratch
+    double* partials = nullptr;
+    unsigned* counter = nullptr;
+    double* red_out = nullptr;  // small device result area
+    double* red_h = nullptr;    // pinned host mirror
+    int part_cap = 0;
+
+    anl::FilterState filt;
+    float* ftmp = nullptr;   // element-field scratch (ne)
+    float* ftmp2 = nullptr;  // element-field scratch (ne)
+};

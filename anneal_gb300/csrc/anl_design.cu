@@ -1,0 +1,533 @@
+// anl_design.cu -- design-variable kernels of one SIMP iteration: density filter,
+// projection, stiffness scale, sensitivity, OC bisection and the history statistics.
+//
+// Element fields are FP32 on the full grid (x fastest, zero on inactive elements); sums
+// that decide the OC bisection and the history values accumulate in FP64.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "anl_ctx.cuh"
+
+namespace anl {
+
+constexpr int DT = 256;
+static inline int dgrid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(kRedBlocks, (n + DT - 1) / DT)); }
+
+// ------------------------------------------------------------------ density filter
+
+// Filter (optimize.py:24-47). One CTA of 32x4x2 threads owns a 32x4x2 tile of elements
+// and stages the tile plus an R-element halo in shared memory.
+enum { F_HS = 0, F_FWD = 1, F_BWD = 2, F_PHYS = 3, F_OCVOL = 4 };
+
+constexpr int FT_X = 32, FT_Y = 4, FT_Z = 2, FT_N = FT_X * FT_Y * FT_Z;
+
+struct FilterArgs {
+    Dims d;
+    int R;
+    const float* w;        // (2R+1)^3 cone weights
+    const uint8_t* active;
+    const float* Hs;
+    const float* in;       // FWD/BWD/PHYS input field
+    float* out;
+    // PHYS
+    const uint8_t* frozen;
+    float* dxp;
+    float beta, eta, t0, t1;
+    // OCVOL: the filtered field is xn(lambda) built on the fly
+    const float* x;
+    const float* dcx;
+    const float* dvx;
+    const float* phi;
+    float lam, move;
+    double* partials;
+    unsigned* counter;
+    double* red_out;
+};
+
+__device__ __forceinline__ float oc_xn(float x, float dcx, float dvx, float lam, float move) {
+    // optimize.py:150-152: ratio = sqrt(max(-dcx,0) / max(dvx*lam, 1e-300)),
+    // xn = clip(x*ratio, max(0, x-mv), min(1, x+mv))
+    const float num = fmaxf(-dcx, 0.f);
+    const float den = dvx * lam;
+    float v;
+    if (den > 1e-30f) v = x * sqrtf(num / den);
+    else v = (num > 0.f && x > 0.f) ? INFINITY : 0.f;  // the FP64 guard 1e-300 makes the ratio huge
+    const float lo = fmaxf(0.f, x - move), hi = fminf(1.f, x + move);
+    return fminf(fmaxf(v, lo), hi);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
+    extern __shared__ float sm[];
+    const Dims d = a.d;
+    const int R = a.R, W = 2 * R + 1;
+    const int TX = FT_X + 2 * R, TY = FT_Y + 2 * R, TZ = FT_Z + 2 * R;
+    float* tile = sm;
+    float* wts = sm + TX * TY * TZ;
+    const int tid = threadIdx.x + FT_X * (threadIdx.y + FT_Y * threadIdx.z);
+    const int i0 = blockIdx.x * FT_X, j0 = blockIdx.y * FT_Y, k0 = blockIdx.z * FT_Z;
+    for (int t = tid; t < W * W * W; t += FT_N) wts[t] = a.w[t];
+    for (int t = tid; t < TX * TY * TZ; t += FT_N) {
+        const int tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
+        const int gi = i0 - R + tx, gj = j0 - R + ty, gk = k0 - R + tz;
+        float v = 0.f;
+        if (gi >= 0 && gj >= 0 && gk >= 0 && gi < d.nx && gj < d.ny && gk < d.nz) {
+            const int64_t e = d.elem(gi, gj, gk);
+            if (a.active[e]) {
+                if (MODE == F_HS) v = 1.f;
+                else if (MODE == F_FWD || MODE == F_PHYS) v = a.in[e];
+                else if (MODE == F_BWD) v = a.in[e] / a.Hs[e];
+                else if (MODE == F_OCVOL) v = a.frozen[e] ? 1.f : oc_xn(a.x[e], a.dcx[e], a.dvx[e], a.lam, a.move);
+            }
+        }
+        tile[t] = v;
+    }
+    __syncthreads();
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y, k = k0 + threadIdx.z;
+    double vol = 0.0;
+    if (i < d.nx && j < d.ny && k < d.nz) {
+        float s = 0.f;
+        for (int dz = 0; dz < W; ++dz)
+            for (int dy = 0; dy < W; ++dy) {
+                const float* row = tile + ((threadIdx.z + dz) * TY + (threadIdx.y + dy)) * TX + threadIdx.x;
+                const float* wr = wts + (dz * W + dy) * W;
+                for (int dx = 0; dx < W; ++dx) s = fmaf(wr[dx], row[dx], s);
+            }
+        const int64_t e = d.elem(i, j, k);
+        const bool act = a.active[e] != 0;
+        if (MODE == F_HS) {
+            a.out[e] = s == 0.f ? 1.f : s;
+        } else if (MODE == F_FWD) {
+            a.out[e] = act ? s / a.Hs[e] : 0.f;
+        } else if (MODE == F_BWD) {
+            a.out[e] = act ? s : 0.f;
+        } else {
+            // physical(): projection (optimize.py:81-87), frozen -> 1 (optimize.py:92)
+            float xt = act ? s / a.Hs[e] : 0.f;
+            float xp = xt, g = 1.f;
+            if (a.beta > 0.f) {
+                const float th = tanhf(a.beta * (xt - a.eta));
+                xp = (a.t0 + th) / (a.t0 + a.t1);
+                g = a.beta * (1.f - th * th) / (a.t0 + a.t1);
+            }
+            if (a.frozen[e]) xp = 1.f;
+            if (!act) {
+                xp = 0.f;
+                g = 0.f;
+            }
+            if (MODE == F_PHYS) {
+                a.out[e] = xp;
+                if (a.dxp) a.dxp[e] = g;
+            } else {
+                vol = act ? (double)a.phi[e] * (double)xp : 0.0;
+            }
+        }
+    }
+    if (MODE == F_OCVOL) {
+        __shared__ double red[FT_N / 32];
+        double v[1] = {vol};
+        block_sum<1, FT_N>(v, red);
+        const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        finish_reduction<1>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out);
+    }
+}
+
+static int launch_filter(anl_ctx* c, int mode, FilterArgs a, cudaStream_t s) {
+    const Dims& d = c->d;
+    a.d = d;
+    a.R = c->filt.R;
+    a.w = c->filt.w;
+    a.active = c->active;
+    a.Hs = c->filt.Hs;
+    const int W = 2 * a.R + 1;
+    const size_t smem = sizeof(float) * ((FT_X + 2 * a.R) * (FT_Y + 2 * a.R) * (FT_Z + 2 * a.R) + W * W * W);
+    dim3 grid(ceil_div(d.nx, FT_X), ceil_div(d.ny, FT_Y), ceil_div(d.nz, FT_Z)), block(FT_X, FT_Y, FT_Z);
+    if (mode == F_OCVOL && (int64_t)grid.x * grid.y * grid.z > c->part_cap) {
+        set_error("filter reduction needs %d blocks, scratch holds %d", grid.x * grid.y * grid.z, c->part_cap);
+        return ANL_ERR_BADARG;
+    }
+    switch (mode) {
+        case F_HS: k_filter<F_HS><<<grid, block, smem, s>>>(a); break;
+        case F_FWD: k_filter<F_FWD><<<grid, block, smem, s>>>(a); break;
+        case F_BWD: k_filter<F_BWD><<<grid, block, smem, s>>>(a); break;
+        case F_PHYS: k_filter<F_PHYS><<<grid, block, smem, s>>>(a); break;
+        case F_OCVOL: k_filter<F_OCVOL><<<grid, block, smem, s>>>(a); break;
+        default: return ANL_ERR_BADARG;
+    }
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
+int filter_init(anl_ctx* c, double r, cudaStream_t s) {
+    int R = (int)std::ceil(r) - 1;
+    if (R < 1) R = 1;
+    if (R > kMaxFilterR || !(r > 0)) {
+        set_error("filter radius %.3f voxels needs a %d-element halo; at most %d is supported", r, R, kMaxFilterR);
+        return ANL_ERR_BADARG;
+    }
+    const int W = 2 * R + 1;
+    std::vector<float> w(W * W * W);
+    for (int dz = -R; dz <= R; ++dz)
+        for (int dy = -R; dy <= R; ++dy)
+            for (int dx = -R; dx <= R; ++dx) {
+                const double v = r - std::sqrt((double)(dx * dx + dy * dy + dz * dz));
+                w[(dx + R) + W * ((dy + R) + W * (dz + R))] = v > 0 ? (float)v : 0.f;
+            }
+    if (c->filt.w) cudaFree(c->filt.w);
+    c->filt.w = nullptr;
+    ANL_CUDA(cudaMalloc(&c->filt.w, sizeof(float) * w.size()));
+    ANL_CUDA(cudaMemcpyAsync(c->filt.w, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, s));
+    c->filt.R = R;
+    c->filt.r = r;
+    FilterArgs a{};
+    a.out = c->filt.Hs;
+    ANL_TRY(launch_filter(c, F_HS, a, s));
+    ANL_CUDA(cudaStreamSynchronize(s));  // the host weights vector goes out of scope
+    c->filt.ready = true;
+    return ANL_OK;
+}
+
+int filter_apply(anl_ctx* c, bool forward, const float* in, float* out, cudaStream_t s) {
+    FilterArgs a{};
+    a.in = in;
+    a.out = out;
+    return launch_filter(c, forward ? F_FWD : F_BWD, a, s);
+}
+
+int physical(anl_ctx* c, const float* x, const uint8_t* frozen, double beta, double eta, float* xphys, float* dxp,
+             cudaStream_t s) {
+    FilterArgs a{};
+    a.in = x;
+    a.out = xphys;
+    a.frozen = frozen;
+    a.dxp = dxp;
+    a.beta = (float)beta;
+    a.eta = (float)eta;
+    if (beta > 0) {
+        a.t0 = (float)std::tanh(beta * eta);
+        a.t1 = (float)std::tanh(beta * (1 - eta));
+    }
+    return launch_filter(c, F_PHYS, a, s);
+}
+
+// ------------------------------------------------------------------ stiffness scale
+
+__global__ void k_escale(int64_t ne, const uint8_t* active, const float* xphys, const float* phi, float E0, float emin,
+                         float p, float* escale) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (active[e]) {
+            const float xp = xphys[e];
+            const float xpp = p == 1.f ? xp : (p == 3.f ? xp * xp * xp : powf(xp, p));
+            v = E0 * phi[e] * (emin + xpp * (1.f - emin));
+        }
+        escale[e] = v;
+    }
+}
+
+int stiffness_scale(anl_ctx* c, const float* xphys, const float* phi, double E0, double emin, double p, float* escale,
+                    cudaStream_t s) {
+    const int64_t ne = c->d.ne();
+    k_escale<<<dgrid(ne), DT, 0, s>>>(ne, c->active, xphys, phi, (float)E0, (float)emin, (float)p, escale);
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
+// ------------------------------------------------------------------ sensitivity
+
+struct KeFull {
+    float k[24 * 24];
+};
+
+constexpr int kMaxCases = 16;
+struct SensArgs {
+    Dims d;
+    const uint8_t* active;
+    const double* u;  // nrhs nodal vectors
+    int nrhs;
+    int64_t stride;   // 3 * nn
+    float coef[kMaxCases];
+    const float* xphys;
+    const float* dxp;
+    const float* phi;
+    float p, emin, E0, h;
+    float* out;       // dc (combined, clipped, times dxp) or ce (energy only)
+    float* dv;        // phi * dxp (optional)
+    int energy_only;
+};
+
+// u_e^T Ke u_e with u_e taken relative to the element's first node (Ke annihilates
+// translations), so FP32 products scale with the strain, not with |u|.
+__device__ __forceinline__ float element_energy(const KeFull& K, const double* u, const Dims& d, int i, int j, int k) {
+    const int64_t n0 = d.node(i, j, k);
+    const int64_t sx = 1, sy = d.nx + 1, sz = (int64_t)(d.nx + 1) * (d.ny + 1);
+    const int64_t off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
+    const double b0 = u[3 * n0], b1 = u[3 * n0 + 1], b2 = u[3 * n0 + 2];
+    float dv[21];
+#pragma unroll
+    for (int a = 1; a < 8; ++a) {
+        const int64_t n = n0 + off[a];
+        dv[3 * (a - 1)] = (float)(u[3 * n] - b0);
+        dv[3 * (a - 1) + 1] = (float)(u[3 * n + 1] - b1);
+        dv[3 * (a - 1) + 2] = (float)(u[3 * n + 2] - b2);
+    }
+    float ce = 0.f;
+#pragma unroll
+    for (int r = 0; r < 21; ++r) {
+        float t = 0.f;
+#pragma unroll
+        for (int q = 0; q < 21; ++q) t = fmaf(K.k[(r + 3) * 24 + q + 3], dv[q], t);
+        ce = fmaf(dv[r], t, ce);
+    }
+    return ce;
+}
+
+__global__ void k_sens(SensArgs a, KeFull K) {
+    const Dims d = a.d;
+    const int64_t ne = d.ne();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (a.active[e]) {
+            const int i = (int)(e % d.nx), j = (int)((e / d.nx) % d.ny), k = (int)(e / ((int64_t)d.nx * d.ny));
+            if (a.energy_only) {
+                v = a.h * element_energy(K, a.u, d, i, j, k);
+            } else {
+                const float xp = a.xphys[e];
+                const float dpow = a.p == 1.f ? 1.f : (a.p == 3.f ? xp * xp : powf(xp, a.p - 1.f));
+                const float pre = -a.p * dpow * (1.f - a.emin) * a.E0 * a.phi[e] * a.h;
+                float dc = 0.f;
+                for (int c = 0; c < a.nrhs; ++c) dc += a.coef[c] * pre * element_energy(K, a.u + c * a.stride, d, i, j, k);
+                dc = fminf(dc, 0.f);
+                v = a.dxp ? dc * a.dxp[e] : dc;
+            }
+        }
+        a.out[e] = v;
+        if (a.dv) a.dv[e] = a.active[e] ? (a.dxp ? a.phi[e] * a.dxp[e] : a.phi[e]) : 0.f;
+    }
+}
+
+int sensitivity(anl_ctx* c, const double* u, int nrhs, const double* coef, const float* xphys, const float* dxp,
+                const float* phi, double p, double emin, double E0, float* out, float* dv, bool energy_only,
+                cudaStream_t s) {
+    if (nrhs < 1 || nrhs > kMaxCases) {
+        set_error("sensitivity supports 1..%d load cases, got %d", kMaxCases, nrhs);
+        return ANL_ERR_BADARG;
+    }
+    SensArgs a{};
+    a.d = c->d;
+    a.active = c->active;
+    a.u = u;
+    a.nrhs = nrhs;
+    a.stride = 3 * c->d.nn();
+    for (int k = 0; k < nrhs; ++k) a.coef[k] = coef ? (float)coef[k] : 1.f;
+    a.xphys = xphys;
+    a.dxp = dxp;
+    a.phi = phi;
+    a.p = (float)p;
+    a.emin = (float)emin;
+    a.E0 = (float)E0;
+    a.h = (float)c->h;
+    a.out = out;
+    a.dv = energy_only ? nullptr : dv;
+    a.energy_only = energy_only ? 1 : 0;
+    KeFull K;
+    for (int t = 0; t < 576; ++t) K.k[t] = (float)c->ke[t];
+    const int64_t ne = c->d.ne();
+    k_sens<<<dgrid(ne), DT, 0, s>>>(a, K);
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
+// ------------------------------------------------------------------ OC update
+
+// sums over design (active, non-frozen) elements: -dcx, dvx, count
+__global__ void k_oc_scale(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* dcx, const float* dvx,
+                           double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[3 * DT / 32];
+    double v[3] = {0, 0, 0};
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
+        if (active[e] && !frozen[e]) {
+            v[0] -= dcx[e];
+            v[1] += dvx[e];
+            v[2] += 1.0;
+        }
+    block_sum<3, DT>(v, sm);
+    finish_reduction<3>(v, blockIdx.x, gridDim.x, partials, counter, out);
+}
+
+// With no projection the volume is linear in xn: vol = sum_j wv_j xn_j + sum_frozen phi,
+// wv = Filter.backward(phi on non-frozen elements). One pass per bisection step.
+__global__ void k_oc_vol_linear(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x,
+                                const float* dcx, const float* dvx, const float* wv, float lam, float move,
+                                double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[DT / 32];
+    Acc2 acc;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
+        if (active[e]) {
+            const float xn = frozen[e] ? 1.f : oc_xn(x[e], dcx[e], dvx[e], lam, move);
+            acc.add_prod(wv[e], xn);
+        }
+    double v[1] = {acc.value()};
+    block_sum<1, DT>(v, sm);
+    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out);
+}
+
+__global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,
+                             double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[DT / 32];
+    double f[1] = {0.0};
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        const bool a = active[e] != 0, fz = frozen[e] != 0;
+        v[e] = a && !fz ? phi[e] : 0.f;
+        if (a && fz) f[0] += phi[e];
+    }
+    block_sum<1, DT>(f, sm);
+    finish_reduction<1>(f, blockIdx.x, gridDim.x, partials, counter, out);
+}
+
+__global__ void k_oc_final(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x, const float* dcx,
+                           const float* dvx, float lam, float move, float* xnew) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
+        xnew[e] = active[e] ? (frozen[e] ? 1.f : oc_xn(x[e], dcx[e], dvx[e], lam, move)) : 0.f;
+}
+
+static int read_red(anl_ctx* c, int nv, cudaStream_t s) {
+    ANL_CUDA(cudaMemcpyAsync(c->red_h, c->red_out, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    return ANL_OK;
+}
+
+int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, const float* phi, const uint8_t* frozen,
+              double move, double beta, double eta, double vtarget, float* xnew, int* steps_out, double* lam_out,
+              cudaStream_t s) {
+    const int64_t ne = c->d.ne();
+    k_oc_scale<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, dcx, dvx, c->partials, c->counter, c->red_out);
+    ANL_LAUNCH_CHECK();
+    ANL_TRY(read_red(c, 3, s));
+    // optimize.py:145
+    double scale = 1.0;
+    const double nd = c->red_h[2];
+    if (nd > 0) {
+        const double mdc = c->red_h[0] / nd, mdv = c->red_h[1] / nd;
+        scale = std::max(mdc / std::max(mdv, 1e-30), 1e-300);
+    }
+    double lo = scale * 1e-8, hi = scale * 1e8;
+    const double mv = beta <= 1 ? move : move / 2;  // optimize.py:151
+    double vfrozen = 0.0;
+    const bool linear = !(beta > 0);
+    if (linear) {
+        k_oc_weights<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, phi, c->ftmp2, c->partials, c->counter, c->red_out);
+        ANL_LAUNCH_CHECK();
+        ANL_TRY(read_red(c, 1, s));
+        vfrozen = c->red_h[0];
+        ANL_TRY(filter_apply(c, false, c->ftmp2, c->ftmp, s));
+    }
+    double lam = std::sqrt(lo * hi);
+    int steps = 0;
+    for (int k = 0; k < 100; ++k) {
+        lam = std::sqrt(lo * hi);
+        double vol;
+        if (linear) {
+            k_oc_vol_linear<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, c->ftmp, (float)lam, (float)mv,
+                                                     c->partials, c->counter, c->red_out);
+            ANL_LAUNCH_CHECK();
+            ANL_TRY(read_red(c, 1, s));
+            vol = c->red_h[0] + vfrozen;
+        } else {
+            FilterArgs a{};
+            a.frozen = frozen;
+            a.beta = (float)beta;
+            a.eta = (float)eta;
+            a.t0 = (float)std::tanh(beta * eta);
+            a.t1 = (float)std::tanh(beta * (1 - eta));
+            a.x = x;
+            a.dcx = dcx;
+            a.dvx = dvx;
+            a.phi = phi;
+            a.lam = (float)lam;
+            a.move = (float)mv;
+            a.partials = c->partials;
+            a.counter = c->counter;
+            a.red_out = c->red_out;
+            ANL_TRY(launch_filter(c, F_OCVOL, a, s));
+            ANL_TRY(read_red(c, 1, s));
+            vol = c->red_h[0];
+        }
+        if (vol > vtarget) lo = lam;
+        else hi = lam;
+        ++steps;
+        if (hi / lo < 1 + 1e-9) break;
+    }
+    k_oc_final<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, (float)lam, (float)mv, xnew);
+    ANL_LAUNCH_CHECK();
+    if (steps_out) *steps_out = steps;
+    if (lam_out) *lam_out = lam;
+    return ANL_OK;
+}
+
+// ------------------------------------------------------------------ history statistics
+
+__global__ void k_stats(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* xold, const float* xnew,
+                        const float* xphys, const float* phi, double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[3 * DT / 32];
+    __shared__ float smax[DT / 32];
+    double v[3] = {0, 0, 0};
+    float mx = 0.f;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        if (!active[e]) continue;
+        const float xp = xphys[e];
+        v[2] += (double)phi[e] * (double)xp;
+        if (!frozen[e]) {
+            mx = fmaxf(mx, fabsf(xnew[e] - xold[e]));
+            if (xp > 0.1f && xp < 0.9f) v[0] += 1.0;
+            v[1] += 1.0;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
+    block_sum<3, DT>(v, sm);
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < DT / 32; ++w) mx = fmaxf(mx, smax[w]);
+    }
+    double vals[4] = {v[0], v[1], v[2], (double)mx};
+    // the max is exact in any order; store it through the same deterministic path
+    __shared__ double res[4];
+    if (threadIdx.x == 0) {
+        partials[(int64_t)blockIdx.x * 4 + 0] = vals[0];
+        partials[(int64_t)blockIdx.x * 4 + 1] = vals[1];
+        partials[(int64_t)blockIdx.x * 4 + 2] = vals[2];
+        partials[(int64_t)blockIdx.x * 4 + 3] = vals[3];
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        if (t == gridDim.x - 1) {
+            __threadfence();
+            double s0 = 0, s1 = 0, s2 = 0, m = 0;
+            for (unsigned b = 0; b < gridDim.x; ++b) {
+                const volatile double* pb = partials + (int64_t)b * 4;
+                s0 += pb[0];
+                s1 += pb[1];
+                s2 += pb[2];
+                m = fmax(m, pb[3]);
+            }
+            res[0] = m;
+            res[1] = s1 > 0 ? s0 / s1 : 0.0;
+            res[2] = s2;
+            res[3] = s1;
+            for (int q = 0; q < 4; ++q) out[q] = res[q];
+            *counter = 0u;
+        }
+    }
+}
+
+int design_stats(anl_ctx* c, const float* xold, const float* xnew, const float* xphys, const float* phi,
+                 const uint8_t* frozen, double* out, cudaStream_t s) {
+    const int64_t ne = c->d.ne();
+    k_stats<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, xold, xnew, xphys, phi, c->partials, c->counter, c->red_out);
+    ANL_LAUNCH_CHECK();
+    ANL_TRY(read_red(c, 4, s));
+    for (int q = 0; q < 4; ++q) out[q] = c->red_h[q];
+    return ANL_OK;
+}
+
+}  // namespace anl

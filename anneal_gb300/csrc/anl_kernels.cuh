@@ -1,0 +1,35 @@
+// anl_kernels.cuh -- launch interfaces shared by the translation units of the library.
+#pragma once
+
+#include "anl_common.cuh"
+
+namespace anl {
+
+// ------------------------------------------------------------------ K u family
+
+enum { KU_APPLY = 0, KU_APPLY_DOT = 1, KU_RESID = 2, KU_CHEB = 3 };
+
+template <class T>
+struct KuArgs {
+    Dims d;
+    int kz = 0;                      // z-layers per CTA (set by the launcher)
+    const float* E = nullptr;        // element scale (already times h), full grid
+    const uint8_t* nmask = nullptr;  // node mask bits (NODE_FREE_*, NODE_USED)
+    const T* u = nullptr;            // input vector (masked: zeros on non-free DOFs)
+    T* y = nullptr;                  // APPLY*: K u; RESID: b - K u
+    const T* b = nullptr;            // RESID, CHEB
+    T* dv = nullptr;                 // CHEB: Chebyshev direction, updated in place
+    T* xout = nullptr;               // CHEB: u + new direction
+    T c1 = T(0), c2 = T(0);          // CHEB: d <- c1 d + c2 D^-1 (b - K u)
+    T kdiag = T(0);                  // diagonal entry of Ke(1) (all 24 are equal)
+    double* partials = nullptr;      // APPLY_DOT reduction scratch
+    unsigned* counter = nullptr;
+    int partial_capacity = 0;
+    double* red_out = nullptr;       // APPLY_DOT: u . K u
+    const int* done = nullptr;       // early-exit flag of the CG loop (may be null)
+};
+
+template <class T>
+int launch_ku(int mode, const KuArgs<T>& a, const KeBlocks<T>& kb, cudaStream_t s);
+
+}  // namespace anl

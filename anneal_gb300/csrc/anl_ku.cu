@@ -1,0 +1,227 @@
+// anl_ku.cu -- matrix-free hex8 operator K u and the kernels fused with it.
+//
+// Replaces the assembled CSR matrix of FEM.assemble (fem.py:198-201) and its SpMV inside
+// scipy's CG (fem.py:224). K = sum_e E_e Ke acts node by node (gather form, no atomics):
+//
+//   (K u)_n = sum_{octants o} E_o * S_o * sum_{delta != 0} B0(delta) * S_o * (u_{n + o.delta} - u_n)
+//
+// o in {-1,+1}^3 picks the element around node n, S_o = diag(o), B0 are the 8 base 3x3
+// blocks of Ke (anl_common.cuh). The difference form uses the zero block-row sums of Ke;
+// it keeps FP32 products proportional to the local strain rather than to |u|, which is
+// what lets the FP32 operator resolve residuals far below |K| |u| eps.
+//
+// Tiling: a CTA of 32x8 threads owns a 32x8 column of nodes and marches up a chunk of
+// z-layers, keeping three node planes (with a one-node halo) and two element planes in
+// shared memory. HBM traffic is u once, y once, E once and the node mask once.
+#include "anl_common.cuh"
+#include "anl_kernels.cuh"
+
+namespace anl {
+
+constexpr int KU_BX = 32, KU_BY = 8;
+constexpr int KU_HX = KU_BX + 2, KU_HY = KU_BY + 2;
+constexpr int KU_EX = KU_BX + 1, KU_EY = KU_BY + 1;
+constexpr int KU_NT = KU_BX * KU_BY;
+
+template <class T>
+struct DotAcc;
+template <>
+struct DotAcc<float> {
+    Acc2 a;
+    __device__ void add(float x, float y) { a.add_prod(x, y); }
+    __device__ double value() const { return a.value(); }
+};
+template <>
+struct DotAcc<double> {
+    double s = 0.0;
+    __device__ void add(double x, double y) { s = fma(x, y, s); }
+    __device__ double value() const { return s; }
+};
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(KU_NT, 2) ku_kernel(KuArgs<T> a, KeBlocks<T> kb) {
+    __shared__ T su[3][KU_HY][KU_HX][3];
+    __shared__ float sE[2][KU_EY][KU_EX];
+    __shared__ double sred[KU_NT / 32];
+    if (a.done != nullptr && *a.done) return;
+
+    const Dims d = a.d;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * KU_BX + tx;
+    const int i0 = blockIdx.x * KU_BX, j0 = blockIdx.y * KU_BY, k0 = blockIdx.z * a.kz;
+    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+
+    auto load_nodes = [&](int slot, int kk) {
+        const bool kin = kk >= 0 && kk < NZn;
+        for (int f = tid; f < KU_HY * KU_HX * 3; f += KU_NT) {
+            const int row = f / (KU_HX * 3);
+            const int w = f - row * (KU_HX * 3);
+            const int c = w / 3, comp = w - 3 * c;
+            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
+            T v = T(0);
+            if (kin && gi >= 0 && gi < NXn && gj >= 0 && gj < NYn) v = a.u[3 * d.node(gi, gj, kk) + comp];
+            su[slot][row][c][comp] = v;
+        }
+    };
+    auto load_elems = [&](int slot, int ke) {
+        const bool kin = ke >= 0 && ke < d.nz;
+        for (int f = tid; f < KU_EY * KU_EX; f += KU_NT) {
+            const int row = f / KU_EX, c = f - row * KU_EX;
+            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
+            float v = 0.f;
+            if (kin && gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny) v = a.E[d.elem(gi, gj, ke)];
+            sE[slot][row][c] = v;
+        }
+    };
+
+    load_nodes(0, k0 - 1);
+    load_nodes(1, k0);
+    load_elems(0, k0 - 1);
+    DotAcc<T> dot;
+    const int i = i0 + tx, j = j0 + ty;
+    const int kend = min(k0 + a.kz, NZn);
+    for (int k = k0; k < kend; ++k) {
+        const int r = k - k0;
+        const int s_lo = r % 3, s_mid = (r + 1) % 3, s_hi = (r + 2) % 3;
+        const int e_lo = r & 1, e_hi = (r + 1) & 1;
+        load_nodes(s_hi, k + 1);
+        load_elems(e_hi, k);
+        __syncthreads();
+        if (i < NXn && j < NYn) {
+            const T* base[3] = {&su[s_lo][0][0][0], &su[s_mid][0][0][0], &su[s_hi][0][0][0]};
+            T un[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) un[c] = su[s_mid][ty + 1][tx + 1][c];
+            // differences to the 26 neighbours, dl[mz+1][my+1][mx+1][c]
+            T dl[3][3][3][3];
+#pragma unroll
+            for (int mz = 0; mz < 3; ++mz)
+#pragma unroll
+                for (int my = 0; my < 3; ++my)
+#pragma unroll
+                    for (int mx = 0; mx < 3; ++mx) {
+                        const T* p = base[mz] + ((ty + my) * KU_HX + (tx + mx)) * 3;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) dl[mz][my][mx][c] = p[c] - un[c];
+                    }
+            T y[3] = {T(0), T(0), T(0)};
+            float esum = 0.f;
+#pragma unroll
+            for (int oct = 0; oct < 8; ++oct) {
+                const int sx = (oct & 1) ? 1 : -1, sy = (oct & 2) ? 1 : -1, sz = (oct & 4) ? 1 : -1;
+                const float Eo = sE[sz > 0 ? e_hi : e_lo][ty + (sy > 0 ? 1 : 0)][tx + (sx > 0 ? 1 : 0)];
+                esum += Eo;
+                T w[3] = {T(0), T(0), T(0)};
+#pragma unroll
+                for (int dlt = 1; dlt < 8; ++dlt) {
+                    const int dx = dlt & 1, dy = (dlt >> 1) & 1, dz = (dlt >> 2) & 1;
+                    const T* dv = dl[1 + sz * dz][1 + sy * dy][1 + sx * dx];
+                    const T t0 = sx > 0 ? dv[0] : -dv[0];
+                    const T t1 = sy > 0 ? dv[1] : -dv[1];
+                    const T t2 = sz > 0 ? dv[2] : -dv[2];
+                    const T* B = kb.blk[dlt];
+#pragma unroll
+                    for (int rr = 0; rr < 3; ++rr) w[rr] += B[3 * rr] * t0 + B[3 * rr + 1] * t1 + B[3 * rr + 2] * t2;
+                }
+                const T Et = T(Eo);
+                y[0] += sx > 0 ? Et * w[0] : -Et * w[0];
+                y[1] += sy > 0 ? Et * w[1] : -Et * w[1];
+                y[2] += sz > 0 ? Et * w[2] : -Et * w[2];
+            }
+            const int64_t n = d.node(i, j, k);
+            const uint8_t nm = a.nmask[n];
+            if (MODE == KU_APPLY || MODE == KU_APPLY_DOT) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const T v = (nm >> c) & 1 ? y[c] : T(0);
+                    a.y[3 * n + c] = v;
+                    if (MODE == KU_APPLY_DOT) dot.add(un[c], v);
+                }
+            } else if (MODE == KU_RESID) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) a.y[3 * n + c] = (nm >> c) & 1 ? a.b[3 * n + c] - y[c] : T(0);
+            } else if (MODE == KU_CHEB) {
+                const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    T dn = T(0), xn = T(0);
+                    if ((nm >> c) & 1) {
+                        const T rc = a.b[3 * n + c] - y[c];
+                        dn = a.c1 * a.dv[3 * n + c] + a.c2 * rc * inv;
+                        xn = un[c] + dn;
+                    }
+                    a.dv[3 * n + c] = dn;
+                    a.xout[3 * n + c] = xn;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (MODE == KU_APPLY_DOT) {
+        double v[1] = {dot.value()};
+        // block_sum uses a flat thread index; reshape the 2D block
+        const int lane = tid & 31, warp = tid >> 5;
+        double s = v[0];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sred[warp] = s;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0;
+            for (int w = 0; w < KU_NT / 32; ++w) t += sred[w];
+            v[0] = t;
+        }
+        const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        const int nb = gridDim.x * gridDim.y * gridDim.z;
+        __shared__ bool last;
+        if (tid == 0) {
+            a.partials[bid] = v[0];
+            __threadfence();
+            last = atomicAdd(a.counter, 1u) == (unsigned)nb - 1;
+        }
+        __syncthreads();
+        if (last && tid == 0) {
+            __threadfence();
+            double t = 0;
+            for (int b = 0; b < nb; ++b) t += ((volatile double*)a.partials)[b];
+            *a.red_out = t;
+            *a.counter = 0u;
+        }
+    }
+}
+
+template <class T>
+int launch_ku(int mode, const KuArgs<T>& args, const KeBlocks<T>& kb, cudaStream_t s) {
+    KuArgs<T> a = args;
+    const Dims& d = a.d;
+    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+    int chunks = ceil_div(NZn, 16);
+    a.kz = ceil_div(NZn, chunks);
+    dim3 grid(ceil_div(NXn, KU_BX), ceil_div(NYn, KU_BY), ceil_div(NZn, a.kz));
+    dim3 block(KU_BX, KU_BY);
+    if (mode == KU_APPLY_DOT && (int64_t)grid.x * grid.y * grid.z > a.partial_capacity) {
+        set_error("K u dot: %d blocks exceed the reduction scratch (%d)", grid.x * grid.y * grid.z,
+                  a.partial_capacity);
+        return ANL_ERR_BADARG;
+    }
+    switch (mode) {
+        case KU_APPLY: ku_kernel<T, KU_APPLY><<<grid, block, 0, s>>>(a, kb); break;
+        case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<grid, block, 0, s>>>(a, kb); break;
+        case KU_RESID: ku_kernel<T, KU_RESID><<<grid, block, 0, s>>>(a, kb); break;
+        case KU_CHEB: ku_kernel<T, KU_CHEB><<<grid, block, 0, s>>>(a, kb); break;
+        default: return ANL_ERR_BADARG;
+    }
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
+int ku_grid_blocks(const Dims& d) {
+    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+    const int chunks = ceil_div(NZn, 16);
+    const int kz = ceil_div(NZn, chunks);
+    return ceil_div(NXn, KU_BX) * ceil_div(NYn, KU_BY) * ceil_div(NZn, kz);
+}
+
+template int launch_ku<float>(int, const KuArgs<float>&, const KeBlocks<float>&, cudaStream_t);
+template int launch_ku<double>(int, const KuArgs<double>&, const KeBlocks<double>&, cudaStream_t);
+
+}  // namespace anl

@@ -1,0 +1,898 @@
+// anl_solver.cu -- geometric-multigrid preconditioned CG on the voxel grid.
+//
+// Replaces FEM.solve (fem.py:206-232): scipy CG with a pyamg smoothed-aggregation V-cycle
+// on the assembled matrix. Here:
+//  * the operator is the matrix-free K u of anl_ku.cu (FP32, or FP64 with ANL_FLAG_FP64);
+//  * the preconditioner is a V-cycle on the voxel hierarchy (element dims halved per level):
+//    coarse element scale = (sum of the 8 children)/4 (their mean at Ke(2h) = 2 Ke(h)),
+//    trilinear prolongation P and restriction P^T, Chebyshev smoothing on D^-1 K with the
+//    spectrum bound from power iteration, and a dense FP64 Cholesky solve on the coarsest
+//    grid (a high-degree Chebyshev sweep if that grid is too large for a dense factor);
+//  * the CG iterate x and right-hand side stay in FP64; the CG scalars come from FP64
+//    reductions (compensated FP32 partials); the residual is replaced by the true
+//    residual b - K x (x split as hi + lo in FP32) periodically and before convergence is
+//    accepted, so the stopping test ||b - K x|| <= rtol ||b|| holds for the true residual;
+//  * beta is the flexible (Polak-Ribiere) form, robust to the FP32 preconditioner;
+//  * every loop kernel checks a device "done" flag, so the host enqueues a few iterations
+//    at a time and synchronises once per chunk.
+#include <algorithm>
+#include <cstring>
+#include <utility>
+
+#include "anl_ctx.cuh"
+
+namespace anl {
+
+constexpr int VT = 256;  // threads of the 1D vector kernels
+
+static inline int vgrid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(kRedBlocks, (n + VT - 1) / VT)); }
+
+// ------------------------------------------------------------------ accumulators
+
+template <class T>
+struct Sum;
+template <>
+struct Sum<float> {
+    Acc2 a;
+    __device__ void prod(float x, float y) { a.add_prod(x, y); }
+    __device__ double get() const { return a.value(); }
+};
+template <>
+struct Sum<double> {
+    double s = 0;
+    __device__ void prod(double x, double y) { s = fma(x, y, s); }
+    __device__ double get() const { return s; }
+};
+
+// ------------------------------------------------------------------ masks and levels
+
+__global__ void k_mask_level0(Dims d, const uint8_t* active, const uint8_t* fixed, uint8_t* nmask) {
+    const int64_t nn = d.nn();
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(n % (d.nx + 1));
+        const int j = (int)((n / (d.nx + 1)) % (d.ny + 1));
+        const int k = (int)(n / ((int64_t)(d.nx + 1) * (d.ny + 1)));
+        bool used = false;
+        for (int o = 0; o < 8 && !used; ++o) {
+            const int ei = i - 1 + (o & 1), ej = j - 1 + ((o >> 1) & 1), ek = k - 1 + ((o >> 2) & 1);
+            if (ei >= 0 && ej >= 0 && ek >= 0 && ei < d.nx && ej < d.ny && ek < d.nz) used = active[d.elem(ei, ej, ek)] != 0;
+        }
+        uint8_t m = 0;
+        if (used) {
+            m = NODE_USED;
+            for (int c = 0; c < 3; ++c)
+                if (!fixed[3 * n + c]) m |= (uint8_t)(1 << c);
+        }
+        nmask[n] = m;
+    }
+}
+
+__global__ void k_eact_coarse(Dims f, Dims c, const uint8_t* ef, uint8_t* ec) {
+    const int64_t ne = c.ne();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        const int I = (int)(e % c.nx), J = (int)((e / c.nx) % c.ny), K = (int)(e / ((int64_t)c.nx * c.ny));
+        uint8_t a = 0;
+        for (int o = 0; o < 8; ++o) {
+            const int i = 2 * I + (o & 1), j = 2 * J + ((o >> 1) & 1), k = 2 * K + ((o >> 2) & 1);
+            if (i < f.nx && j < f.ny && k < f.nz) a |= ef[f.elem(i, j, k)];
+        }
+        ec[e] = a ? 1 : 0;
+    }
+}
+
+// A coarse DOF is fixed when a used fine node within one fine spacing has that DOF fixed.
+__global__ void k_mask_coarse(Dims f, Dims c, const uint8_t* nmf, const uint8_t* eac, uint8_t* nmc) {
+    const int64_t nn = c.nn();
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const int I = (int)(n % (c.nx + 1));
+        const int J = (int)((n / (c.nx + 1)) % (c.ny + 1));
+        const int K = (int)(n / ((int64_t)(c.nx + 1) * (c.ny + 1)));
+        bool used = false;
+        for (int o = 0; o < 8 && !used; ++o) {
+            const int ei = I - 1 + (o & 1), ej = J - 1 + ((o >> 1) & 1), ek = K - 1 + ((o >> 2) & 1);
+            if (ei >= 0 && ej >= 0 && ek >= 0 && ei < c.nx && ej < c.ny && ek < c.nz) used = eac[c.elem(ei, ej, ek)] != 0;
+        }
+        uint8_t m = 0;
+        if (used) {
+            uint8_t fixed = 0;
+            for (int dk = -1; dk <= 1; ++dk)
+                for (int dj = -1; dj <= 1; ++dj)
+                    for (int di = -1; di <= 1; ++di) {
+                        const int i = 2 * I + di, j = 2 * J + dj, k = 2 * K + dk;
+                        if (i < 0 || j < 0 || k < 0 || i > f.nx || j > f.ny || k > f.nz) continue;
+                        const uint8_t fm = nmf[f.node(i, j, k)];
+                        if (fm & NODE_USED) fixed |= (uint8_t)(~fm & 7);
+                    }
+            m = (uint8_t)(NODE_USED | (~fixed & 7));
+        }
+        nmc[n] = m;
+    }
+}
+
+__global__ void k_count_free(int64_t nn, const uint8_t* nmask, double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[VT / 32];
+    double v[1] = {0.0};
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x)
+        v[0] += (double)__popc(nmask[n] & 7);
+    block_sum<1, VT>(v, sm);
+    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out);
+}
+
+__global__ void k_level0_E(int64_t ne, const float* escale, const uint8_t* active, float h, float* E) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
+        E[e] = active[e] ? h * escale[e] : 0.f;
+}
+
+__global__ void k_coarsen_E(Dims f, Dims c, const float* Ef, float* Ec) {
+    const int64_t ne = c.ne();
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        const int I = (int)(e % c.nx), J = (int)((e / c.nx) % c.ny), K = (int)(e / ((int64_t)c.nx * c.ny));
+        float s = 0.f;
+        for (int o = 0; o < 8; ++o) {
+            const int i = 2 * I + (o & 1), j = 2 * J + ((o >> 1) & 1), k = 2 * K + ((o >> 2) & 1);
+            if (i < f.nx && j < f.ny && k < f.nz) s += Ef[f.elem(i, j, k)];
+        }
+        Ec[e] = 0.25f * s;
+    }
+}
+
+__global__ void k_diag(Dims d, const float* E, float kdiag, float* diag) {
+    const int64_t nn = d.nn();
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(n % (d.nx + 1));
+        const int j = (int)((n / (d.nx + 1)) % (d.ny + 1));
+        const int k = (int)(n / ((int64_t)(d.nx + 1) * (d.ny + 1)));
+        float s = 0.f;
+        for (int o = 0; o < 8; ++o) {
+            const int ei = i - 1 + (o & 1), ej = j - 1 + ((o >> 1) & 1), ek = k - 1 + ((o >> 2) & 1);
+            if (ei >= 0 && ej >= 0 && ek >= 0 && ei < d.nx && ej < d.ny && ek < d.nz) s += E[d.elem(ei, ej, ek)];
+        }
+        diag[n] = kdiag * s;
+    }
+}
+
+// ------------------------------------------------------------------ transfers
+
+template <class T>
+__global__ void k_restrict(Dims f, Dims c, const T* rf, const uint8_t* nmc, T* bc, const int* done) {
+    if (done && *done) return;
+    const int64_t nn = c.nn();
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const int I = (int)(n % (c.nx + 1));
+        const int J = (int)((n / (c.nx + 1)) % (c.ny + 1));
+        const int K = (int)(n / ((int64_t)(c.nx + 1) * (c.ny + 1)));
+        T acc[3] = {T(0), T(0), T(0)};
+        for (int dk = -1; dk <= 1; ++dk) {
+            const int k = 2 * K + dk;
+            if (k < 0 || k > f.nz) continue;
+            const T wk = dk == 0 ? T(1) : T(0.5);
+            for (int dj = -1; dj <= 1; ++dj) {
+                const int j = 2 * J + dj;
+                if (j < 0 || j > f.ny) continue;
+                const T wj = dj == 0 ? wk : wk * T(0.5);
+                for (int di = -1; di <= 1; ++di) {
+                    const int i = 2 * I + di;
+                    if (i < 0 || i > f.nx) continue;
+                    const T w = di == 0 ? wj : wj * T(0.5);
+                    const int64_t fn = f.node(i, j, k);
+                    acc[0] += w * rf[3 * fn];
+                    acc[1] += w * rf[3 * fn + 1];
+                    acc[2] += w * rf[3 * fn + 2];
+                }
+            }
+        }
+        const uint8_t m = nmc[n];
+        for (int cc = 0; cc < 3; ++cc) bc[3 * n + cc] = (m >> cc) & 1 ? acc[cc] : T(0);
+    }
+}
+
+template <class T>
+__global__ void k_prolong_add(Dims f, Dims c, const T* xc, const uint8_t* nmf, T* xf, const int* done) {
+    if (done && *done) return;
+    const int64_t nn = f.nn();
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(n % (f.nx + 1));
+        const int j = (int)((n / (f.nx + 1)) % (f.ny + 1));
+        const int k = (int)(n / ((int64_t)(f.nx + 1) * (f.ny + 1)));
+        const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
+        const T wi = (i & 1) ? T(0.5) : T(1), wj = (j & 1) ? T(0.5) : T(1), wk = (k & 1) ? T(0.5) : T(1);
+        T acc[3] = {T(0), T(0), T(0)};
+        for (int ck = 0; ck < nk; ++ck)
+            for (int cj = 0; cj < nj; ++cj)
+                for (int ci = 0; ci < ni; ++ci) {
+                    const int64_t cn = c.node(i / 2 + ci, j / 2 + cj, k / 2 + ck);
+                    const T w = wi * wj * wk;
+                    acc[0] += w * xc[3 * cn];
+                    acc[1] += w * xc[3 * cn + 1];
+                    acc[2] += w * xc[3 * cn + 2];
+                }
+        const uint8_t m = nmf[n];
+        for (int cc = 0; cc < 3; ++cc)
+            if ((m >> cc) & 1) xf[3 * n + cc] += acc[cc];
+    }
+}
+
+// x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
+template <class T>
+__global__ void k_cheb_first(int64_t nn, const T* b, const float* diag, const uint8_t* nmask, T c2, T* x, T* dv,
+                             const int* done) {
+    if (done && *done) return;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t m = nmask[n];
+        const float dg = diag[n];
+        const T inv = dg > 0.f ? T(1) / T(dg) : T(0);
+        for (int c = 0; c < 3; ++c) {
+            const T v = (m >> c) & 1 ? c2 * b[3 * n + c] * inv : T(0);
+            x[3 * n + c] = v;
+            dv[3 * n + c] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ power iteration
+
+__device__ __forceinline__ float hash01(uint64_t i) {
+    uint64_t z = i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)((z >> 40) * (1.0 / 16777216.0));
+}
+
+template <class T>
+__global__ void k_power_init(int64_t nn, const uint8_t* nmask, T* v) {
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t m = nmask[n];
+        for (int c = 0; c < 3; ++c) v[3 * n + c] = (m >> c) & 1 ? T(0.5f + hash01(3 * n + c)) : T(0);
+    }
+}
+
+// v = D^-1 y, rescaled by 1/scale to keep magnitudes near one
+template <class T>
+__global__ void k_jacobi_scale(int64_t nn, const T* y, const float* diag, const uint8_t* nmask, T scale, T* v) {
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t m = nmask[n];
+        const float dg = diag[n];
+        for (int c = 0; c < 3; ++c) v[3 * n + c] = ((m >> c) & 1) && dg > 0.f ? y[3 * n + c] / (T(dg) * scale) : T(0);
+    }
+}
+
+template <class T>
+__global__ void k_dot_diag(int64_t nn, const T* v, const float* diag, double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[VT / 32];
+    Sum<T> s;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const T dg = T(diag[n]);
+        for (int c = 0; c < 3; ++c) s.prod(v[3 * n + c] * dg, v[3 * n + c]);
+    }
+    double val[1] = {s.get()};
+    block_sum<1, VT>(val, sm);
+    finish_reduction<1>(val, blockIdx.x, gridDim.x, partials, counter, out);
+}
+
+// ------------------------------------------------------------------ coarsest grid (FP64)
+
+// Dense K of the coarsest level, one thread per entry (deterministic: each entry sums
+// the elements shared by its two nodes in a fixed order). Non-free rows/cols -> identity.
+__global__ void k_assemble_dense(Dims d, const float* E, const uint8_t* nmask, const double* ke, int n, double* A) {
+    const int64_t total = (int64_t)n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int row = (int)(t / n), col = (int)(t % n);
+        const int64_t N = row / 3, M = col / 3;
+        const int ci = row % 3, cj = col % 3;
+        const bool fr = (nmask[N] >> ci) & 1, fc = (nmask[M] >> cj) & 1;
+        if (!fr || !fc) {
+            A[t] = row == col ? 1.0 : 0.0;
+            continue;
+        }
+        const int Ni = (int)(N % (d.nx + 1)), Nj = (int)((N / (d.nx + 1)) % (d.ny + 1)),
+                  Nk = (int)(N / ((int64_t)(d.nx + 1) * (d.ny + 1)));
+        const int Mi = (int)(M % (d.nx + 1)), Mj = (int)((M / (d.nx + 1)) % (d.ny + 1)),
+                  Mk = (int)(M / ((int64_t)(d.nx + 1) * (d.ny + 1)));
+        double s = 0.0;
+        if (abs(Ni - Mi) <= 1 && abs(Nj - Mj) <= 1 && abs(Nk - Mk) <= 1) {
+            for (int o = 0; o < 8; ++o) {
+                const int ei = Ni - 1 + (o & 1), ej = Nj - 1 + ((o >> 1) & 1), ek = Nk - 1 + ((o >> 2) & 1);
+                if (ei < 0 || ej < 0 || ek < 0 || ei >= d.nx || ej >= d.ny || ek >= d.nz) continue;
+                const int bi = Mi - ei, bj = Mj - ej, bk = Mk - ek;
+                if (bi < 0 || bi > 1 || bj < 0 || bj > 1 || bk < 0 || bk > 1) continue;
+                const int ai = Ni - ei, aj = Nj - ej, ak = Nk - ek;
+                // local node numbering LOCAL (fem.py:20-21): bottom face counter-clockwise
+                const int la = (ak << 2) | (aj ? (ai ? 2 : 3) : (ai ? 1 : 0));
+                const int lb = (bk << 2) | (bj ? (bi ? 2 : 3) : (bi ? 1 : 0));
+                s += (double)E[d.elem(ei, ej, ek)] * ke[(3 * la + ci) * 24 + 3 * lb + cj];
+            }
+        }
+        A[t] = s;
+    }
+}
+
+// In-place lower Cholesky factor of the n x n SPD matrix A (one CTA, right-looking).
+__global__ void __launch_bounds__(1024) k_cholesky(double* A, int n, int* flag) {
+    __shared__ double piv;
+    for (int j = 0; j < n; ++j) {
+        if (threadIdx.x == 0) {
+            const double a = A[(int64_t)j * n + j];
+            if (!(a > 0.0)) {
+                *flag = 1;
+                piv = 1.0;
+            } else {
+                piv = sqrt(a);
+            }
+            A[(int64_t)j * n + j] = piv;
+        }
+        __syncthreads();
+        const double p = piv;
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) A[(int64_t)i * n + j] /= p;
+        __syncthreads();
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        for (int gi = j + 1 + warp; gi < n; gi += nw) {
+            const double lij = A[(int64_t)gi * n + j];
+            for (int gk = j + 1 + lane; gk <= gi; gk += 32) A[(int64_t)gi * n + gk] -= lij * A[(int64_t)gk * n + j];
+        }
+        __syncthreads();
+    }
+}
+
+// Column c of A^-1 from the Cholesky factor L (lower triangle of A): one CTA per column.
+__global__ void __launch_bounds__(128) k_chol_inverse(const double* L, double* Ainv, int n) {
+    extern __shared__ double xs[];
+    const int c = blockIdx.x;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = i == c ? 1.0 : 0.0;
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {  // L y = e_c
+        const double yj = xs[j] / L[(int64_t)j * n + j];
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = yj;
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) xs[i] -= L[(int64_t)i * n + j] * yj;
+        __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {  // L^T x = y
+        const double xj = xs[j] / L[(int64_t)j * n + j];
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = xj;
+        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] -= L[(int64_t)j * n + i] * xj;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i];
+}
+
+// x = A^-1 b on the coarsest grid (FP64), one warp per row.
+template <class T>
+__global__ void k_coarse_apply(const double* Ainv, int n, const T* b, const uint8_t* nmask, T* x, const int* done) {
+    if (done && *done) return;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int row = warp; row < n; row += nw) {
+        double s = 0.0;
+        for (int c = lane; c < n; c += 32) s += Ainv[(int64_t)row * n + c] * (double)b[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) x[row] = (nmask[row / 3] >> (row % 3)) & 1 ? T(s) : T(0);
+    }
+}
+
+// ------------------------------------------------------------------ CG vector kernels
+
+__global__ void k_mask_copy_d(int64_t nn, const double* in, const uint8_t* nmask, double* out) {
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t m = nmask[n];
+        for (int c = 0; c < 3; ++c) out[3 * n + c] = (m >> c) & 1 ? in[3 * n + c] : 0.0;
+    }
+}
+
+template <class T>
+__global__ void k_mask_copy_t(int64_t nn, const T* in, const uint8_t* nmask, T* out) {
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t m = nmask[n];
+        for (int c = 0; c < 3; ++c) out[3 * n + c] = (m >> c) & 1 ? in[3 * n + c] : T(0);
+    }
+}
+
+__global__ void k_dot_d(int64_t n, const double* a, const double* b, double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[VT / 32];
+    double v[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[0] = fma(a[i], b[i], v[0]);
+    block_sum<1, VT>(v, sm);
+    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out);
+}
+
+// x (FP64) -> hi + lo in T
+template <class T>
+__global__ void k_split(int64_t n, const double* x, T* hi, T* lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        const T h = T(v);
+        hi[i] = h;
+        lo[i] = T(v - (double)h);
+    }
+}
+
+// r = b - y1 - y2 (y2 may be null), ||r||^2; sets the CG state from the true residual.
+template <class T>
+__global__ void k_true_resid(int64_t n, const double* b, const T* y1, const T* y2, T* r, PcgScalars* sc,
+                             int set_state, double* partials, unsigned* counter) {
+    __shared__ double sm[VT / 32];
+    double v[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double ri = b[i] - (double)y1[i];
+        if (y2) ri -= (double)y2[i];
+        r[i] = T(ri);
+        v[0] = fma(ri, ri, v[0]);
+    }
+    block_sum<1, VT>(v, sm);
+    __shared__ double res[1];
+    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res)) {
+        if (threadIdx.x == 0) {
+            sc->rr_true = res[0];
+            if (set_state) {
+                sc->rr = res[0];
+                if (!isfinite(res[0])) {
+                    sc->done = 3;
+                    sc->nonfinite = 1;
+                } else {
+                    sc->done = res[0] <= sc->tol2 ? 1 : 0;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_init_scalars(PcgScalars* sc, double rtol, int maxiter, const double* bb) {
+    sc->bb = *bb;
+    sc->tol2 = rtol * rtol * (*bb);
+    sc->iters = 0;
+    sc->done = 0;
+    sc->nonfinite = 0;
+    sc->maxiter = maxiter;
+    sc->rz[0] = sc->rz[1] = 0.0;
+    sc->alpha = 0.0;
+    sc->zq = 0.0;
+    sc->pq = 0.0;
+}
+
+template <class T>
+__global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgScalars* sc, const int* restart,
+                             double* partials, unsigned* counter) {
+    __shared__ double sm[2 * VT / 32];
+    if (sc->done) return;
+    const bool rs = *restart != 0;
+    Sum<T> a, b;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T zi = z[i];
+        a.prod(r[i], zi);
+        if (!rs) b.prod(zi, q[i]);
+    }
+    double v[2] = {a.get(), b.get()};
+    block_sum<2, VT>(v, sm);
+    __shared__ double res[2];
+    if (finish_reduction<2>(v, blockIdx.x, gridDim.x, partials, counter, res)) {
+        if (threadIdx.x == 0) {
+            const int it = sc->iters;
+            sc->rz[it & 1] = res[0];
+            sc->zq = res[1];
+            if (!isfinite(res[0]) || !isfinite(res[1])) {
+                sc->done = 3;
+                sc->nonfinite = 1;
+            } else if (!(res[0] > 0.0)) {
+                sc->done = 4;
+            }
+        }
+    }
+}
+
+template <class T>
+__global__ void k_pupdate(int64_t n, const T* z, T* p, const PcgScalars* sc, const int* restart) {
+    if (sc->done) return;
+    const int it = sc->iters;
+    if (*restart) {
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = z[i];
+        return;
+    }
+    const double beta = -sc->alpha * sc->zq / sc->rz[(it + 1) & 1];
+    const T bt = T(beta);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = z[i] + bt * p[i];
+}
+
+template <class T>
+__global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgScalars* sc, int* restart,
+                       double* partials, unsigned* counter) {
+    __shared__ double sm[VT / 32];
+    if (sc->done) return;
+    const int it = sc->iters;
+    const double pq = sc->pq;
+    const double alpha = sc->rz[it & 1] / pq;
+    const bool bad = !(pq > 0.0) || !isfinite(alpha);
+    Sum<T> rr;
+    if (!bad) {
+        const T at = T(alpha);
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            const T pi = p[i];
+            x[i] = fma(alpha, (double)pi, x[i]);
+            const T ri = r[i] - at * q[i];
+            r[i] = ri;
+            rr.prod(ri, ri);
+        }
+    }
+    double v[1] = {rr.get()};
+    block_sum<1, VT>(v, sm);
+    __shared__ double res[1];
+    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res)) {
+        if (threadIdx.x == 0) {
+            sc->alpha = alpha;
+            sc->rr = res[0];
+            sc->iters = it + 1;
+            *restart = 0;
+            if (bad) {
+                if (isfinite(pq) && isfinite(alpha)) sc->done = 4;
+                else {
+                    sc->done = 3;
+                    sc->nonfinite = 1;
+                }
+            } else if (!isfinite(res[0])) {
+                sc->done = 3;
+                sc->nonfinite = 1;
+            } else if (res[0] <= sc->tol2) {
+                sc->done = 1;
+            } else if (it + 1 >= sc->maxiter) {
+                sc->done = 2;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+template <class T>
+static KeBlocks<T> blocks_of(const anl_ctx* c);
+template <>
+KeBlocks<float> blocks_of<float>(const anl_ctx* c) { return c->kbf; }
+template <>
+KeBlocks<double> blocks_of<double>(const anl_ctx* c) { return c->kbd; }
+
+template <class T>
+static KuArgs<T> ku_args(anl_ctx* c, const Level& L) {
+    KuArgs<T> a;
+    a.d = L.d;
+    a.E = L.E;
+    a.nmask = L.nmask;
+    a.kdiag = T(c->kdiag);
+    a.partials = c->partials;
+    a.counter = c->counter;
+    a.partial_capacity = c->part_cap;
+    return a;
+}
+
+template <class T>
+static int apply_level(anl_ctx* c, const Level& L, const T* u, T* y, cudaStream_t s, double* dot_out = nullptr,
+                       const int* done = nullptr) {
+    KuArgs<T> a = ku_args<T>(c, L);
+    a.u = u;
+    a.y = y;
+    a.done = done;
+    a.red_out = dot_out;
+    return launch_ku<T>(dot_out ? KU_APPLY_DOT : KU_APPLY, a, blocks_of<T>(c), s);
+}
+
+// Largest eigenvalue of D^-1 K on a level: 15 power steps, then the Rayleigh quotient
+// v.Kv / v.Dv. The estimate approaches lambda_max from below (measured 0.9-0.97 of it).
+template <class T>
+static int estimate_lmax(anl_ctx* c, Level& L, cudaStream_t s) {
+    const int64_t nn = L.d.nn();
+    T* v = (T*)L.x;
+    T* y = (T*)L.r;
+    k_power_init<T><<<vgrid(nn), VT, 0, s>>>(nn, L.nmask, v);
+    ANL_LAUNCH_CHECK();
+    double scale = 1.0;
+    for (int it = 0; it < 15; ++it) {
+        ANL_TRY(apply_level<T>(c, L, v, y, s));
+        k_jacobi_scale<T><<<vgrid(nn), VT, 0, s>>>(nn, y, L.diag, L.nmask, T(scale), v);
+        ANL_LAUNCH_CHECK();
+        scale = 3.0;  // typical growth per step; keeps values O(1)
+    }
+    ANL_TRY(apply_level<T>(c, L, v, y, s, c->red_out));
+    k_dot_diag<T><<<vgrid(nn), VT, 0, s>>>(nn, v, L.diag, c->partials, c->counter, c->red_out + 1);
+    ANL_LAUNCH_CHECK();
+    ANL_CUDA(cudaMemcpyAsync(c->red_h, c->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    const double num = c->red_h[0], den = c->red_h[1];
+    L.lmax = (den > 0 && std::isfinite(num / den) && num > 0) ? num / den : 4.0;
+    return ANL_OK;
+}
+
+static int coarse_factor(anl_ctx* c, cudaStream_t s) {
+    Level& L = c->lev.back();
+    const int n = c->nc;
+    const int64_t total = (int64_t)n * n;
+    k_assemble_dense<<<(int)std::min<int64_t>(4096, (total + 255) / 256), 256, 0, s>>>(L.d, L.E, L.nmask, c->ke_d, n, c->A);
+    ANL_LAUNCH_CHECK();
+    ANL_CUDA(cudaMemsetAsync(c->flag_d, 0, sizeof(int), s));
+    k_cholesky<<<1, 1024, 0, s>>>(c->A, n, c->flag_d);
+    ANL_LAUNCH_CHECK();
+    k_chol_inverse<<<n, 128, n * sizeof(double), s>>>(c->A, c->Ainv, n);
+    ANL_LAUNCH_CHECK();
+    int flag = 0;
+    ANL_CUDA(cudaMemcpyAsync(&flag, c->flag_d, sizeof(int), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    if (flag) {
+        set_error("coarse-grid matrix is not positive definite (the part may be unsupported)");
+        return ANL_ERR_SINGULAR;
+    }
+    c->coarse_ready = true;
+    return ANL_OK;
+}
+
+// Refresh the hierarchy's element scales from the level-0 scales; with `rebuild` also
+// re-estimate the smoother spectra and refactor the coarsest grid.
+template <class T>
+static int update_hierarchy(anl_ctx* c, bool rebuild, cudaStream_t s) {
+    for (size_t l = 0; l < c->lev.size(); ++l) {
+        Level& L = c->lev[l];
+        if (l > 0) {
+            const Level& F = c->lev[l - 1];
+            k_coarsen_E<<<vgrid(L.d.ne()), VT, 0, s>>>(F.d, L.d, F.E, L.E);
+            ANL_LAUNCH_CHECK();
+        }
+        k_diag<<<vgrid(L.d.nn()), VT, 0, s>>>(L.d, L.E, (float)c->kdiag, L.diag);
+        ANL_LAUNCH_CHECK();
+    }
+    const bool first = !c->coarse_ready;
+    if (rebuild || first) {
+        const size_t nsm = c->dense_coarse ? c->lev.size() - 1 : c->lev.size();
+        for (size_t l = 0; l < nsm; ++l) ANL_TRY(estimate_lmax<T>(c, c->lev[l], s));
+        if (c->dense_coarse) ANL_TRY(coarse_factor(c, s));
+        else c->coarse_ready = true;
+    }
+    return ANL_OK;
+}
+
+struct ChebCoef {
+    double c1, c2;
+};
+
+static void cheb_coefs(double lmax, int degree, ChebCoef* out) {
+    const double hi = 1.1 * lmax, lo = 0.1 * lmax;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    double rho_old = 1.0 / sigma;
+    out[0] = {0.0, 1.0 / theta};
+    for (int k = 1; k < degree; ++k) {
+        const double rho = 1.0 / (2.0 * sigma - rho_old);
+        out[k] = {rho * rho_old, 2.0 * rho / delta};
+        rho_old = rho;
+    }
+}
+
+// degree Chebyshev steps on level L; x_is_zero uses the elementwise first step.
+template <class T>
+static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* done, cudaStream_t s) {
+    ChebCoef cf[32];
+    cheb_coefs(L.lmax, degree, cf);
+    int k0 = 0;
+    if (x_is_zero) {
+        k_cheb_first<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const T*)L.b, L.diag, L.nmask, T(cf[0].c2),
+                                                         (T*)L.x, (T*)L.dv, done);
+        ANL_LAUNCH_CHECK();
+        k0 = 1;
+    }
+    for (int k = k0; k < degree; ++k) {
+        KuArgs<T> a = ku_args<T>(c, L);
+        a.u = (const T*)L.x;
+        a.b = (const T*)L.b;
+        a.dv = (T*)L.dv;
+        a.xout = (T*)L.xt;
+        a.c1 = T(cf[k].c1);
+        a.c2 = T(cf[k].c2);
+        a.done = done;
+        ANL_TRY(launch_ku<T>(KU_CHEB, a, blocks_of<T>(c), s));
+        std::swap(L.x, L.xt);
+    }
+    return ANL_OK;
+}
+
+template <class T>
+static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
+    Level& L = c->lev[l];
+    if (l + 1 == c->lev.size()) {
+        if (c->dense_coarse) {
+            const int n = c->nc;
+            k_coarse_apply<T><<<std::max(1, (n * 32 + 255) / 256), 256, 0, s>>>(c->Ainv, n, (const T*)L.b, L.nmask,
+                                                                             (T*)L.x, done);
+            ANL_LAUNCH_CHECK();
+            return ANL_OK;
+        }
+        return smooth<T>(c, L, 16, true, done, s);
+    }
+    Level& C = c->lev[l + 1];
+    ANL_TRY(smooth<T>(c, L, c->mg_degree, true, done, s));
+    KuArgs<T> a = ku_args<T>(c, L);
+    a.u = (const T*)L.x;
+    a.b = (const T*)L.b;
+    a.y = (T*)L.r;
+    a.done = done;
+    ANL_TRY(launch_ku<T>(KU_RESID, a, blocks_of<T>(c), s));
+    k_restrict<T><<<vgrid(C.d.nn()), VT, 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
+    ANL_LAUNCH_CHECK();
+    ANL_TRY(vcycle<T>(c, l + 1, done, s));
+    k_prolong_add<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
+    ANL_LAUNCH_CHECK();
+    ANL_TRY(smooth<T>(c, L, c->mg_degree, false, done, s));
+    return ANL_OK;
+}
+
+// r = b - K x with x (FP64, ctx->xbuf) split into hi + lo; updates the CG state.
+template <class T>
+static int true_residual(anl_ctx* c, int set_state, cudaStream_t s) {
+    Level& L0 = c->lev[0];
+    const int64_t n = 3 * L0.d.nn();
+    T* r = (T*)L0.b;
+    if (sizeof(T) == 8) {
+        ANL_TRY(apply_level<T>(c, L0, (const T*)(const void*)c->xbuf, (T*)c->y1, s));
+        k_true_resid<T><<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (const T*)c->y1, nullptr, r, c->sc, set_state, c->partials,
+                                                c->counter);
+    } else {
+        k_split<T><<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (T*)c->xhi, (T*)c->xlo);
+        ANL_LAUNCH_CHECK();
+        ANL_TRY(apply_level<T>(c, L0, (const T*)c->xhi, (T*)c->y1, s));
+        ANL_TRY(apply_level<T>(c, L0, (const T*)c->xlo, (T*)c->y2, s));
+        k_true_resid<T><<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (const T*)c->y1, (const T*)c->y2, r, c->sc, set_state,
+                                                c->partials, c->counter);
+    }
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
+template <class T>
+static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxiter, int* iters, double* relres,
+                   cudaStream_t s) {
+    Level& L0 = c->lev[0];
+    const int64_t nn = L0.d.nn(), n = 3 * nn;
+    int* restart = c->flag_d + 1;
+    k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, f, L0.nmask, c->bbuf);
+    k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, x, L0.nmask, c->xbuf);
+    k_dot_d<<<vgrid(n), VT, 0, s>>>(n, c->bbuf, c->bbuf, c->partials, c->counter, c->red_out);
+    ANL_LAUNCH_CHECK();
+    k_init_scalars<<<1, 1, 0, s>>>(c->sc, rtol, maxiter, c->red_out);
+    ANL_LAUNCH_CHECK();
+    ANL_TRY(true_residual<T>(c, 1, s));
+    const int one = 1;
+    ANL_CUDA(cudaMemcpyAsync(restart, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    *iters = 0;
+    if (c->sc_h->bb == 0.0) {
+        ANL_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+        *relres = 0.0;
+        return ANL_OK;
+    }
+    const int* done = &c->sc->done;
+    int last_replace = 0;
+    int status = ANL_OK;
+    const int chunk = 4;
+    while (true) {
+        if (c->sc_h->done == 0) {
+            for (int k = 0; k < chunk; ++k) {
+                ANL_TRY(vcycle<T>(c, 0, done, s));
+                const T* z = (const T*)L0.x;
+                k_dots_rz_zq<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)L0.b, z, (const T*)c->q, c->sc, restart,
+                                                         c->partials, c->counter);
+                k_pupdate<T><<<vgrid(n), VT, 0, s>>>(n, z, (T*)c->p, c->sc, restart);
+                ANL_LAUNCH_CHECK();
+                ANL_TRY(apply_level<T>(c, L0, (const T*)c->p, (T*)c->q, s, &c->sc->pq, done));
+                k_axpy<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)c->p, (const T*)c->q, c->xbuf, (T*)L0.b, c->sc, restart,
+                                                  c->partials, c->counter);
+                ANL_LAUNCH_CHECK();
+            }
+            ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+            ANL_CUDA(cudaStreamSynchronize(s));
+        }
+        const PcgScalars& h = *c->sc_h;
+        if (h.done == 3) {
+            status = ANL_ERR_NONFINITE;
+            break;
+        }
+        if (h.done == 4) {
+            status = ANL_ERR_BREAKDOWN;
+            break;
+        }
+        const bool want_check = h.done == 1 || h.done == 2 || h.iters - last_replace >= 50;
+        if (!want_check) continue;
+        // true-residual replacement; accept convergence only on the true residual
+        ANL_TRY(true_residual<T>(c, 1, s));
+        ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        ANL_CUDA(cudaStreamSynchronize(s));
+        last_replace = c->sc_h->iters;
+        if (c->sc_h->done == 1) break;
+        if (c->sc_h->done == 3) {
+            status = ANL_ERR_NONFINITE;
+            break;
+        }
+        if (c->sc_h->iters >= maxiter) {
+            status = ANL_ERR_MAXITER;
+            break;
+        }
+        // not converged: the replaced residual carries on (done was cleared)
+    }
+    *iters = c->sc_h->iters;
+    *relres = c->sc_h->bb > 0 ? std::sqrt(std::max(c->sc_h->rr_true, 0.0) / c->sc_h->bb) : 0.0;
+    ANL_CUDA(cudaMemcpyAsync(x, c->xbuf, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return status;
+}
+
+// ------------------------------------------------------------------ entry points used by the C API
+
+int solver_setup_domain(anl_ctx* c, const uint8_t* active, const uint8_t* fixed, cudaStream_t s) {
+    Level& L0 = c->lev[0];
+    ANL_CUDA(cudaMemcpyAsync(c->active, active, L0.d.ne(), cudaMemcpyDeviceToDevice, s));
+    ANL_CUDA(cudaMemcpyAsync(L0.eact, active, L0.d.ne(), cudaMemcpyDeviceToDevice, s));
+    k_mask_level0<<<vgrid(L0.d.nn()), VT, 0, s>>>(L0.d, active, fixed, L0.nmask);
+    ANL_LAUNCH_CHECK();
+    for (size_t l = 1; l < c->lev.size(); ++l) {
+        Level& F = c->lev[l - 1];
+        Level& C = c->lev[l];
+        k_eact_coarse<<<vgrid(C.d.ne()), VT, 0, s>>>(F.d, C.d, F.eact, C.eact);
+        k_mask_coarse<<<vgrid(C.d.nn()), VT, 0, s>>>(F.d, C.d, F.nmask, C.eact, C.nmask);
+        ANL_LAUNCH_CHECK();
+    }
+    k_count_free<<<vgrid(L0.d.nn()), VT, 0, s>>>(L0.d.nn(), L0.nmask, c->partials, c->counter, c->red_out);
+    ANL_LAUNCH_CHECK();
+    ANL_CUDA(cudaMemcpyAsync(c->red_h, c->red_out, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    c->nfree = (int64_t)c->red_h[0];
+    c->domain_set = true;
+    c->coarse_ready = false;
+    return ANL_OK;
+}
+
+int solver_set_escale(anl_ctx* c, const float* escale, cudaStream_t s) {
+    Level& L0 = c->lev[0];
+    k_level0_E<<<vgrid(L0.d.ne()), VT, 0, s>>>(L0.d.ne(), escale, c->active, (float)c->h, L0.E);
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
+int solver_apply(anl_ctx* c, const float* escale, const void* u, void* y, cudaStream_t s) {
+    ANL_TRY(solver_set_escale(c, escale, s));
+    Level& L0 = c->lev[0];
+    const int64_t nn = L0.d.nn();
+    if (c->fp64) {
+        k_mask_copy_t<double><<<vgrid(nn), VT, 0, s>>>(nn, (const double*)u, L0.nmask, (double*)c->tmp);
+        ANL_LAUNCH_CHECK();
+        return apply_level<double>(c, L0, (const double*)c->tmp, (double*)y, s);
+    }
+    k_mask_copy_t<float><<<vgrid(nn), VT, 0, s>>>(nn, (const float*)u, L0.nmask, (float*)c->tmp);
+    ANL_LAUNCH_CHECK();
+    return apply_level<float>(c, L0, (const float*)c->tmp, (float*)y, s);
+}
+
+int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, int nrhs, double rtol, int maxiter,
+                 int rebuild, int* iters, double* relres, cudaStream_t s) {
+    ANL_TRY(solver_set_escale(c, escale, s));
+    if (c->fp64) ANL_TRY(update_hierarchy<double>(c, rebuild != 0, s));
+    else ANL_TRY(update_hierarchy<float>(c, rebuild != 0, s));
+    const int64_t n = 3 * c->lev[0].d.nn();
+    int worst = ANL_OK;
+    for (int k = 0; k < nrhs; ++k) {
+        int st = c->fp64 ? pcg_one<double>(c, f + k * n, x + k * n, rtol, maxiter, iters + k, relres + k, s)
+                         : pcg_one<float>(c, f + k * n, x + k * n, rtol, maxiter, iters + k, relres + k, s);
+        if (st == ANL_ERR_CUDA) return st;
+        if (st != ANL_OK && worst == ANL_OK) worst = st;
+    }
+    if (worst == ANL_ERR_MAXITER) set_error("CG did not reach rtol %.3g in %d iterations", rtol, maxiter);
+    if (worst == ANL_ERR_NONFINITE) set_error("a non-finite value appeared in CG");
+    if (worst == ANL_ERR_BREAKDOWN) set_error("CG breakdown: the operator is not positive definite on the free DOFs");
+    return worst;
+}
+
+int solver_dot(anl_ctx* c, const double* a, const double* b, double* out, cudaStream_t s) {
+    const int64_t n = 3 * c->lev[0].d.nn();
+    k_dot_d<<<vgrid(n), VT, 0, s>>>(n, a, b, c->partials, c->counter, c->red_out);
+    ANL_LAUNCH_CHECK();
+    ANL_CUDA(cudaMemcpyAsync(c->red_h, c->red_out, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    *out = c->red_h[0];
+    return ANL_OK;
+}
+
+}  // namespace anl

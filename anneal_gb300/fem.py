@@ -1,0 +1,236 @@
+"""Voxel FEM with the interface of anneal's fem.py (anneal 0.3.0), solved on the GPU.
+
+``Grid``, ``hex8_matrices``, ``FEM`` and ``SolverError`` keep the reference's names,
+arguments and return types (fem.py:20-263), so callers written for the reference run
+unchanged. What changes underneath: there is no CSR matrix. ``FEM.assemble`` returns a
+lightweight operator that holds the element scales on the device, and ``FEM.solve`` runs
+the multigrid-preconditioned CG of the CUDA library (libanneal_gb300.so). Solves with
+rtol >= 1e-7 run in FP32 with FP64 CG scalars and solution; tighter tolerances run in FP64.
+"""
+import time
+
+import numpy as np
+import torch
+
+from .context import Context, require_cuda, to_dev
+from . import _native as N
+
+LOCAL = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                  [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+
+FP32_RTOL_FLOOR = 1e-7
+
+
+class SolverError(RuntimeError):
+    """Raised where the reference raises it (fem.py:24-25, 138-139, 225-229)."""
+
+
+SOLVER_MESSAGE = ("The solver did not converge in {maxiter} iterations. Usual causes: the part can move "
+                  "or turn freely (add a fixed anchor, or fix more directions on one), or the design has "
+                  "pieces held only by near-empty voxels (raise volumeFraction or iterations).")
+
+
+def elasticity_D(nu):
+    """Isotropic D for E = 1, Voigt order xx yy zz xy yz zx, engineering shear (fem.py:36-43)."""
+    lam = nu / ((1 + nu) * (1 - 2 * nu))
+    mu = 1.0 / (2 * (1 + nu))
+    D = np.zeros((6, 6))
+    D[:3, :3] = lam
+    D[np.arange(3), np.arange(3)] = lam + 2 * mu
+    D[np.arange(3, 6), np.arange(3, 6)] = mu
+    return D
+
+
+def _strain_matrix(point, h):
+    """6x24 strain-displacement matrix of the trilinear brick at a point of [-1, 1]^3."""
+    s = 2.0 * LOCAL - 1.0
+    xi = np.asarray(point, float)
+    # dN_a/dxi_d = s_ad/8 * prod over the other two axes (1 + s_a xi)
+    g = np.empty((8, 3))
+    for d in range(3):
+        o1, o2 = [a for a in range(3) if a != d]
+        g[:, d] = s[:, d] * (1 + s[:, o1] * xi[o1]) * (1 + s[:, o2] * xi[o2]) / 8.0
+    g /= h / 2.0
+    B = np.zeros((6, 24))
+    cols = 3 * np.arange(8)
+    B[0, cols] = g[:, 0]
+    B[1, cols + 1] = g[:, 1]
+    B[2, cols + 2] = g[:, 2]
+    B[3, cols], B[3, cols + 1] = g[:, 1], g[:, 0]
+    B[4, cols + 1], B[4, cols + 2] = g[:, 2], g[:, 1]
+    B[5, cols], B[5, cols + 2] = g[:, 2], g[:, 0]
+    return B
+
+
+def hex8_matrices(nu, h=1.0):
+    """(Ke, B0, D) for a cube of side h, E = 1: Ke by 2x2x2 Gauss quadrature, B0 at the
+    centre (fem.py:71-84)."""
+    D = elasticity_D(nu)
+    g = 1.0 / np.sqrt(3.0)
+    pts = np.array(np.meshgrid([-g, g], [-g, g], [-g, g], indexing="ij")).reshape(3, -1).T
+    ke = np.zeros((24, 24))
+    for p in pts:
+        B = _strain_matrix(p, h)
+        ke += B.T @ D @ B * (h / 2.0) ** 3
+    return ke, _strain_matrix((0.0, 0.0, 0.0), h), D
+
+
+class Grid:
+    """Regular voxel grid; element (i,j,k) spans origin + h*[i,i+1] x ... (fem.py:87-127).
+    Elements and nodes are numbered x fastest."""
+
+    def __init__(self, shape, h, origin):
+        self.shape = tuple(int(s) for s in shape)
+        self.nx, self.ny, self.nz = self.shape
+        self.h = float(h)
+        self.origin = np.asarray(origin, dtype=float)
+        self.nelem = self.nx * self.ny * self.nz
+        self.nnode = (self.nx + 1) * (self.ny + 1) * (self.nz + 1)
+        self._noff = LOCAL[:, 0] + (self.nx + 1) * (LOCAL[:, 1] + (self.ny + 1) * LOCAL[:, 2])
+
+    def elem_ijk(self, e):
+        e = np.asarray(e)
+        return e % self.nx, (e // self.nx) % self.ny, e // (self.nx * self.ny)
+
+    def element_nodes(self, e):
+        i, j, k = self.elem_ijk(e)
+        first = i + (self.nx + 1) * (j + (self.ny + 1) * k)
+        return first[:, None] + self._noff[None, :]
+
+    def node_coords(self, n):
+        n = np.asarray(n)
+        ijk = np.stack([n % (self.nx + 1), (n // (self.nx + 1)) % (self.ny + 1),
+                        n // ((self.nx + 1) * (self.ny + 1))], axis=-1)
+        return self.origin + self.h * ijk
+
+    def elem_centers(self, e=None):
+        e = np.arange(self.nelem) if e is None else e
+        return self.origin + self.h * (np.stack(self.elem_ijk(e), axis=-1) + 0.5)
+
+    def to3d(self, flat):
+        """Flat element array (x fastest) -> array indexed [i, j, k]."""
+        return np.asarray(flat).reshape(self.nz, self.ny, self.nx).transpose(2, 1, 0)
+
+    def to1d(self, arr3):
+        return np.asarray(arr3).transpose(2, 1, 0).ravel()
+
+
+class StiffnessOperator:
+    """What ``FEM.assemble`` returns: the element scales on the device, applied matrix-free.
+    ``K @ u_red`` works on reduced (free-DOF) vectors like the reference's CSR matrix."""
+
+    def __init__(self, fem, Ee):
+        self.fem = fem
+        self.Ee = np.asarray(Ee, float)
+        full = np.zeros(fem.grid.nelem)
+        full[fem.act] = self.Ee
+        self.escale = to_dev(full, torch.float32)
+        self.shape = (fem.nfree, fem.nfree)
+
+    def __matmul__(self, u_red):
+        ctx = self.fem._ctx(fp64=True)
+        u = torch.zeros(ctx.ndof, dtype=torch.float64, device="cuda")
+        u[self.fem._free_t] = to_dev(u_red, torch.float64)
+        y = torch.empty_like(u)
+        ctx.apply_K(self.escale, u, y)
+        return y[self.fem._free_t].cpu().numpy()
+
+    dot = __matmul__
+
+
+class FEM:
+    """Linear elastic solve on the active voxels of a grid (fem.py:130-263)."""
+
+    def __init__(self, grid, active, fixed_dofs, nu, log=None):
+        require_cuda()
+        t0 = time.time()
+        self.grid = grid
+        self.nu = float(nu)
+        self.log = log or (lambda *a: None)
+        self.act = np.flatnonzero(active)
+        if self.act.size == 0:
+            raise SolverError("No active voxels: the design space is empty.")
+        self.ke, self.B0, self.D = hex8_matrices(nu, grid.h)
+        act = np.zeros(grid.nelem, np.uint8)
+        act[self.act] = 1
+        fixed = np.zeros(3 * grid.nnode, np.uint8)
+        fixed[np.asarray(fixed_dofs, dtype=np.int64)] = 1
+        self.active_t = to_dev(act, torch.uint8)
+        self.fixed_t = to_dev(fixed, torch.uint8)
+        self._ctxs = {}
+        ctx = self._ctx(fp64=False)
+        self._mask_t = ctx.free_mask().bool()
+        self.free = np.flatnonzero(self._mask_t.cpu().numpy())
+        self._free_t = torch.as_tensor(self.free, device="cuda")
+        self.nfree = self.free.size
+        self.nnz = None  # no assembled matrix
+        self.amg_builds = 0
+        self.cg_iters = []
+        self.relres = []
+        self.log(f"  system: {self.act.size:,} elements, {self.nfree:,} free dofs, "
+                 f"matrix-free on the GPU, built in {time.time() - t0:.1f} s")
+
+    def _ctx(self, fp64):
+        key = "fp64" if fp64 else "fp32"
+        if key not in self._ctxs:
+            c = Context(self.grid.shape, self.grid.h, self.nu, fp64=fp64)
+            c.set_domain(self.active_t, self.fixed_t)
+            self._ctxs[key] = c
+        return self._ctxs[key]
+
+    @property
+    def edof(self):
+        en = self.grid.element_nodes(self.act)
+        return (3 * en[:, :, None] + np.arange(3)).reshape(-1, 24)
+
+    def assemble(self, Ee):
+        """Ee: stiffness scale per active element (fem.py:198-201)."""
+        return StiffnessOperator(self, Ee)
+
+    def reduce_load(self, F_global):
+        return np.asarray(F_global)[self.free]
+
+    def expand(self, u_red):
+        u = np.zeros(3 * self.grid.nnode)
+        u[self.free] = u_red
+        return u
+
+    def solve_device(self, escale, F, X, rtol=1e-8, maxiter=2000, rebuild=True):
+        """Device-level solve: F, X (nrhs, 3*nnode) float64 CUDA tensors, X holds the
+        initial guesses and receives the solutions. Raises SolverError like fem.py:225-229."""
+        ctx = self._ctx(fp64=rtol < FP32_RTOL_FLOOR)
+        st, iters, relres = ctx.solve(escale, F, X, rtol, maxiter, rebuild)
+        if rebuild:
+            self.amg_builds += 1
+        if st != N.ANL_OK:
+            raise SolverError(SOLVER_MESSAGE.format(maxiter=maxiter))
+        self.cg_iters.extend(iters)
+        self.relres.extend(relres)
+        return iters
+
+    def solve(self, K, F_list, x0_list=None, rebuild=True, rtol=1e-8, maxiter=2000):
+        """fem.py:206-232: reduced loads in, reduced displacements out."""
+        nd = 3 * self.grid.nnode
+        F = torch.zeros((len(F_list), nd), dtype=torch.float64, device="cuda")
+        X = torch.zeros_like(F)
+        for i, f in enumerate(F_list):
+            F[i, self._free_t] = to_dev(f, torch.float64)
+            if x0_list is not None and x0_list[i] is not None:
+                X[i, self._free_t] = to_dev(x0_list[i], torch.float64)
+        self.solve_device(K.escale, F, X, rtol=rtol, maxiter=maxiter, rebuild=rebuild)
+        Xh = X[:, self._free_t].cpu().numpy()
+        if not np.all(np.isfinite(Xh)):
+            raise SolverError(SOLVER_MESSAGE.format(maxiter=maxiter))
+        return [Xh[i].copy() for i in range(len(F_list))]
+
+    def element_energy(self, u_full):
+        """u_e^T ke u_e per active element (fem.py:239-242)."""
+        ctx = self._ctx(fp64=False)
+        ce = torch.empty(self.grid.nelem, dtype=torch.float32, device="cuda")
+        ctx.element_energy(to_dev(u_full, torch.float64), ce)
+        return ce.cpu().numpy().astype(float)[self.act]
+
+    def close(self):
+        for c in self._ctxs.values():
+            c.close()
+        self._ctxs = {}

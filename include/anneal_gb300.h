@@ -1,0 +1,140 @@
+/*
+ * anneal_gb300.h -- C ABI of the GB300 (sm_103a) voxel SIMP library.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream, returns an int
+ * status (ANL_OK = 0) and allocates nothing except inside anl_ctx_create. Arrays:
+ *
+ *   element fields  N_e = nx*ny*nz values, x fastest (fem.py:87-127), zero on inactive
+ *                   elements; float unless stated
+ *   nodal vectors   3*N_n values, N_n = (nx+1)(ny+1)(nz+1), DOF = 3*node + c (fem.py:143),
+ *                   double unless stated; non-free DOFs read as zero and are written as zero
+ *
+ * Each declaration names the reference function it replaces (anneal 0.3.0, path:line).
+ */
+#ifndef ANNEAL_GB300_H
+#define ANNEAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct anl_ctx anl_ctx;
+typedef void* anl_stream_t; /* a cudaStream_t; NULL is the legacy default stream */
+
+enum {
+    ANL_OK = 0,
+    ANL_ERR_MAXITER = 1,   /* CG did not reach rtol in maxiter iterations (fem.py:225-229) */
+    ANL_ERR_NONFINITE = 2, /* a non-finite value appeared in the solve (fem.py:225) */
+    ANL_ERR_BREAKDOWN = 3, /* p.Kp <= 0: the operator is not positive definite */
+    ANL_ERR_BADARG = 4,
+    ANL_ERR_CUDA = 5,
+    ANL_ERR_SINGULAR = 6, /* coarse-grid factorisation failed */
+    ANL_ERR_NOMEM = 7,
+    ANL_ERR_STATE = 8 /* a call that needs anl_set_domain / anl_filter_init came first */
+};
+
+enum { ANL_FLAG_FP64 = 1 /* K u, smoothers and CG vectors in FP64 (default: FP32) */ };
+
+int anl_version(void);
+/* Text of the last error in the calling thread ("" if none). */
+const char* anl_last_error(void);
+
+/* ---------------------------------------------------------------- context (FEM) */
+
+/* Replaces FEM.__init__ (fem.py:133-196) minus the CSR build: the operator stays matrix-free.
+   Allocates the solver workspaces (multigrid hierarchy, CG vectors, reduction scratch). */
+int anl_ctx_create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, int flags);
+void anl_ctx_destroy(anl_ctx* ctx);
+
+/* Free-DOF rule of fem.py:142-155: a DOF is free when its node is touched by an active
+   element and the DOF is not fixed. active: uint8 per element; fixed: uint8 per DOF.
+   Writes the number of free DOFs to *nfree_h (host). */
+int anl_set_domain(anl_ctx* ctx, const uint8_t* active, const uint8_t* fixed, int64_t* nfree_h,
+                   anl_stream_t stream);
+
+/* Free-DOF mask as uint8 per DOF (1 = free): FEM.free (fem.py:150) in full-grid form. */
+int anl_free_mask(anl_ctx* ctx, uint8_t* mask, anl_stream_t stream);
+
+/* ---------------------------------------------------------------- operator and solve */
+
+/* y = K u with K = sum_e escale[e] Ke(h): replaces FEM.assemble (fem.py:198-201) followed by
+   K @ u. escale is the per-element stiffness scale Ee (optimize.py:118), float. u and y are
+   float (default context) or double (ANL_FLAG_FP64). */
+int anl_apply_K(anl_ctx* ctx, const float* escale, const void* u, void* y, anl_stream_t stream);
+
+/* Replaces FEM.solve (fem.py:206-232): solves K x = f for nrhs right-hand sides, one after
+   another, by CG preconditioned with a geometric-multigrid V-cycle, each to
+   ||f - K x|| <= rtol ||f|| checked on the true residual. f and x are nrhs consecutive
+   nodal vectors (double); x holds the initial guesses on entry (x0_list). rebuild != 0
+   re-estimates the smoother spectra and refactors the coarse grid (the reference's AMG
+   rebuild, fem.py:207-216); otherwise the last ones are kept. iters / relres (host arrays
+   of nrhs) receive the CG iterations and final true relative residuals. Returns
+   ANL_ERR_MAXITER or ANL_ERR_NONFINITE where the reference raises SolverError. */
+int anl_solve(anl_ctx* ctx, const float* escale, const double* f, double* x, int nrhs, double rtol,
+              int maxiter, int rebuild, int* iters, double* relres, anl_stream_t stream);
+
+/* sum over DOFs of a[i] * b[i] (double vectors): the compliance f @ u (optimize.py:125). */
+int anl_dot(anl_ctx* ctx, const double* a, const double* b, double* out_h, anl_stream_t stream);
+
+/* ---------------------------------------------------------------- sensitivity */
+
+/* ce[e] = u_e^T Ke(h) u_e on active elements: FEM.element_energy (fem.py:239-242). */
+int anl_element_energy(anl_ctx* ctx, const double* u, float* ce, anl_stream_t stream);
+
+/* Fused sensitivity (optimize.py:126-141 up to the filter backward):
+     dc  = sum_c coef[c] * (-p xphys^(p-1) (1 - emin) E0 phi ce_c),  ce_c = u_c^T Ke u_c
+     out = min(dc, 0) * dxp
+     dv  = phi * dxp          (the argument of the volume filter backward, optimize.py:142)
+   u: nrhs (<= 16) nodal vectors; coef: host array of nrhs combination weights (w for "sum",
+   the p-norm coefficients for "worst"). dxp may be NULL (projection off: dxp = 1); dv may
+   be NULL. */
+int anl_sensitivity(anl_ctx* ctx, const double* u, int nrhs, const double* coef, const float* xphys,
+                    const float* dxp, const float* phi, double p, double emin, double E0, float* out,
+                    float* dv, anl_stream_t stream);
+
+/* escale[e] = E0 * phi (emin + xphys^p (1 - emin)) on active elements, zero elsewhere: the
+   stiffness scale Ee of optimize.py:118 (anl_apply_K / anl_solve apply Ke(h) = h Ke(1)). */
+int anl_stiffness_scale(anl_ctx* ctx, const float* xphys, const float* phi, double E0, double emin,
+                        double p, float* escale, anl_stream_t stream);
+
+/* ---------------------------------------------------------------- density filter */
+
+/* Filter.__init__ (optimize.py:25-34): cone weights max(0, r - |d|) on a (2R+1)^3 box,
+   R = max(ceil(r) - 1, 1) (R <= 5), Hs = conv(active) with zeros set to 1. */
+int anl_filter_init(anl_ctx* ctx, double r_vox, anl_stream_t stream);
+/* Filter.forward (optimize.py:41-43): out = conv(in * active) / Hs on active elements. */
+int anl_filter_fwd(anl_ctx* ctx, const float* in, float* out, anl_stream_t stream);
+/* Filter.backward (optimize.py:45-47): out = conv(in / Hs) * active. */
+int anl_filter_bwd(anl_ctx* ctx, const float* in, float* out, anl_stream_t stream);
+
+/* physical (optimize.py:81-93): xphys = project(filter(x)), frozen elements set to 1;
+   dxp = d project / d xt (NULL to skip). beta <= 0: no projection. */
+int anl_physical(anl_ctx* ctx, const float* x, const uint8_t* frozen, double beta, double eta,
+                 float* xphys, float* dxp, anl_stream_t stream);
+
+/* ---------------------------------------------------------------- OC update */
+
+/* Optimality-criteria bisection (optimize.py:144-161) on the active elements: lambda is
+   bisected geometrically in [1e-8, 1e8] * scale (scale = mean(-dcx)/mean(dvx) over design
+   elements), at most 100 steps, until hi/lo < 1 + 1e-9; the volume sum(phi * physical(xn))
+   is accumulated in FP64. xnew receives the last evaluated xn (as the reference keeps it).
+   steps_h / lambda_h (host, may be NULL) receive the step count and the last lambda. */
+int anl_oc_update(anl_ctx* ctx, const float* x, const float* dcx, const float* dvx, const float* phi,
+                  const uint8_t* frozen, double move, double beta, double eta, double vtarget,
+                  float* xnew, int* steps_h, double* lambda_h, anl_stream_t stream);
+
+/* Per-iteration history values (optimize.py:162-167), all over active elements:
+   out_h[0] = max |xnew - xold| over design (non-frozen) elements (change)
+   out_h[1] = fraction of design elements with 0.1 < xphys < 0.9 (grey)
+   out_h[2] = sum phi * xphys (volume)
+   out_h[3] = number of design elements */
+int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const float* xphys,
+                     const float* phi, const uint8_t* frozen, double* out_h, anl_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ANNEAL_GB300_H */

@@ -1,0 +1,268 @@
+"""Generate the golden fixtures in this folder by running the reference implementation.
+
+The reference is anneal 0.3.0 (pure Python). Its hot path lives in ``anneal/fem.py`` and
+``anneal/optimize.py``. Two of its third-party imports are absent here and get stubs:
+
+* ``pyamg`` (>=5.0, pyproject.toml:14): only a CG preconditioner
+  (fem.py:212-215). The stub returns a Jacobi preconditioner. CG is still run to the
+  reference's own relative residual, so converged answers do not depend on the stub
+  beyond that tolerance.
+* ``trimesh`` (>=4.0): imported at module level by geometry.py. The hot path never
+  calls it, so the stub is an empty module.
+
+Everything else (Ke, CSR assembly, scipy CG, the ndimage filter, the SIMP loop, OC,
+the validation checks V1-V6) is the reference's unchanged code.
+
+Run from the repository root, in a container that holds the reference tree:
+
+    python tests/golden/make_golden.py [--ref /path/to/reference] [--skip-config1]
+
+The config-1 fixture (48x24x24, 50 SIMP iterations, CG at rtol 1e-8 with Jacobi) takes
+several minutes of CPU time. The other fixtures take seconds.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def install_stubs(ref_root):
+    import scipy.sparse.linalg as spla
+
+    pyamg = types.ModuleType("pyamg")
+
+    class _Jacobi:
+        def __init__(self, K):
+            self.d = K.diagonal().copy()
+
+        def aspreconditioner(self, cycle="V"):
+            d = self.d
+            return spla.LinearOperator((d.size, d.size), matvec=lambda x: x / d)
+
+    pyamg.smoothed_aggregation_solver = lambda K, **kw: _Jacobi(K)
+    sys.modules["pyamg"] = pyamg
+    sys.modules["trimesh"] = types.ModuleType("trimesh")
+    sys.path.insert(0, ref_root)
+    import anneal.fem as fem
+    import anneal.optimize as optimize
+    import anneal.validate as validate
+    return fem, optimize, validate
+
+
+def patch_simp_rtol(fem_mod, rtol):
+    """simp() hard-codes rtol=1e-6 (optimize.py:122); wrap FEM.solve to force another rtol.
+    Returns a callable that restores the original method."""
+    orig = fem_mod.FEM.solve
+
+    def wrapper(self, K, F_list, x0_list=None, rebuild=True, rtol=None, maxiter=None):
+        return orig(self, K, F_list, x0_list=x0_list, rebuild=rebuild, rtol=rtol_forced,
+                    maxiter=20000)
+
+    rtol_forced = rtol
+    fem_mod.FEM.solve = wrapper
+
+    def restore():
+        fem_mod.FEM.solve = orig
+    return restore
+
+
+def cantilever(fem_mod, nx, ny, nz, edge_z=0.0):
+    """Clamp every node on x=0; total -1 in z spread over the nodes of the x=nx, z=edge_z line."""
+    g = fem_mod.Grid((nx, ny, nz), 1.0, (0, 0, 0))
+    n = np.arange(g.nnode)
+    p = g.node_coords(n)
+    clamp = n[p[:, 0] < 1e-9]
+    fixed = (3 * clamp[:, None] + np.arange(3)).ravel()
+    tip = n[(abs(p[:, 0] - nx) < 1e-9) & (abs(p[:, 2] - edge_z) < 1e-9)]
+    F = np.zeros(3 * g.nnode)
+    F[3 * tip + 2] = -1.0 / tip.size
+    return g, fixed, F
+
+
+def gen_ke(fem):
+    out = {}
+    for tag, nu, h in (("a", 0.3, 1.0), ("b", 0.3, 0.5), ("c", 0.25, 2.0)):
+        ke, B0, D = fem.hex8_matrices(nu, h)
+        out[f"ke_{tag}"] = ke
+        out[f"B0_{tag}"] = B0
+        out[f"D_{tag}"] = D
+        out[f"nu_{tag}"] = nu
+        out[f"h_{tag}"] = h
+    np.savez_compressed(os.path.join(HERE, "ke.npz"), **out)
+
+
+def gen_fem_small(fem):
+    """Assembled K @ u, element energy and a tight solve on a small ragged domain."""
+    rng = np.random.default_rng(7)
+    g = fem.Grid((7, 5, 4), 1.0, (0, 0, 0))
+    i, j, k = g.elem_ijk(np.arange(g.nelem))
+    active = ~((i >= 4) & (k >= 2))            # an L-shaped domain: inactive voids
+    active &= rng.random(g.nelem) > 0.08        # plus a few random holes
+    act = np.flatnonzero(active)
+    n = np.arange(g.nnode)
+    p = g.node_coords(n)
+    clamp = n[(p[:, 0] < 1e-9) & (p[:, 2] < 2.5)]
+    fixed = np.concatenate([3 * clamp, 3 * clamp + 1, 3 * clamp + 2,
+                            3 * n[(p[:, 0] < 1e-9) & (p[:, 2] > 2.5)] + 2])
+    model = fem.FEM(g, active, fixed, 0.3)
+    Ee = np.exp(rng.normal(0.0, 1.0, act.size)) * 0.5
+    Ee[rng.random(act.size) < 0.2] = 1e-9      # some near-void elements
+    K = model.assemble(Ee)
+    u_red = rng.normal(0.0, 1.0, model.nfree)
+    y_red = K @ u_red
+    ce = model.element_energy(model.expand(u_red))
+    F = np.zeros(3 * g.nnode)
+    tip = n[(abs(p[:, 0] - 7) < 1e-9) & (p[:, 2] < 1e-9)]
+    F[3 * tip + 2] = -1.0 / tip.size
+    F[3 * tip + 1] = 0.25 / tip.size
+    Fr = model.reduce_load(F)
+    Ks = model.assemble(np.where(Ee < 1e-6, 1e-3, Ee))
+    sol = model.solve(Ks, [Fr], rtol=1e-12, maxiter=20000)[0]
+    np.savez_compressed(os.path.join(HERE, "fem_small.npz"), shape=np.array(g.shape), h=g.h,
+                        active=active, fixed=fixed, Ee=Ee, free=model.free, u_red=u_red,
+                        y_red=y_red, ce=ce, F=F, Ee_solve=np.where(Ee < 1e-6, 1e-3, Ee),
+                        u_sol=sol, compliance=float(Fr @ sol), nnz=model.nnz)
+
+
+def gen_filter(optimize, fem):
+    rng = np.random.default_rng(11)
+    g = fem.Grid((9, 7, 6), 1.0, (0, 0, 0))
+    active = rng.random(g.nelem) > 0.15
+    act = np.flatnonzero(active)
+    out = {"shape": np.array(g.shape), "active": active}
+    x = rng.random(act.size)
+    d = rng.normal(0, 1, act.size)
+    out["x"] = x
+    out["d"] = d
+    for tag, r in (("r15", 1.5), ("r20", 2.0), ("r26", 2.6), ("r31", 3.1)):
+        f = optimize.Filter(g, active, r)
+        out[f"fwd_{tag}"] = f.forward(x)
+        out[f"bwd_{tag}"] = f.backward(d)
+        out[f"k_{tag}"] = f.k
+        out[f"Hs_{tag}"] = g.to1d(f.Hs)
+    np.savez_compressed(os.path.join(HERE, "filter.npz"), **out)
+
+
+def _hist_arrays(hist):
+    keys = ("objective", "p", "beta", "volumeFraction", "change", "grey")
+    out = {f"h_{k}": np.array([h[k] for h in hist], float) for k in keys}
+    out["h_compliance"] = np.array([h["compliance"] for h in hist], float)
+    out["h_amg"] = np.array([h["amgRebuilt"] for h in hist], bool)
+    return out
+
+
+def gen_simp_small(fem, optimize, rtol=None):
+    """Default SIMP path (penalty ramp, projection continuation, frozen, partial fill).
+    With ``rtol`` set, every CG solve inside simp runs to that tolerance instead of 1e-6."""
+    restore = patch_simp_rtol(fem, rtol) if rtol else (lambda: None)
+    tag = "simp_small_tight" if rtol else "simp_small"
+    g, fixed, F = cantilever(fem, 16, 8, 8, edge_z=0.0)
+    i, j, k = g.elem_ijk(np.arange(g.nelem))
+    active = ~((i >= 10) & (k >= 5))
+    fill = np.ones(g.nelem)
+    fill[(k == 7) & active] = 0.6
+    fill[~active] = 0.0
+    frozen = (i == 15) & (k <= 1)
+    logs = []
+    res = optimize.simp(g, fill, active, frozen, fixed, {"down": F}, {"down": 1.0}, 70000.0, 0.33, 0.3,
+                        iters=24, r_mm=None, log=logs.append)
+    restore()
+    np.savez_compressed(os.path.join(HERE, f"{tag}.npz"), shape=np.array(g.shape), fill=fill,
+                        active=active, frozen=frozen, fixed=fixed, F=F, E0=70000.0, nu=0.33, vf=0.3,
+                        iters=24, x=res["x"], rMM=res["rMM"], rtol=rtol or 1e-6,
+                        **_hist_arrays(res["history"]))
+    with open(os.path.join(HERE, f"{tag}_log.txt"), "w") as fh:
+        fh.write("\n".join(logs) + "\n")
+
+
+def gen_simp_worst(fem, optimize):
+    """Two load cases combined by the p-norm ('worst'), warm start from a previous design.
+    CG runs to rtol 1e-10 so the fixture pins the loop, not the preconditioner."""
+    restore = patch_simp_rtol(fem, 1e-10)
+    g, fixed, F1 = cantilever(fem, 12, 6, 6, edge_z=0.0)
+    n = np.arange(g.nnode)
+    p = g.node_coords(n)
+    tip = n[(abs(p[:, 0] - 12) < 1e-9) & (abs(p[:, 2] - 6) < 1e-9)]
+    F2 = np.zeros(3 * g.nnode)
+    F2[3 * tip + 1] = 0.5 / tip.size
+    active = np.ones(g.nelem, bool)
+    fill = np.ones(g.nelem)
+    frozen = np.zeros(g.nelem, bool)
+    rng = np.random.default_rng(3)
+    x0 = np.clip(0.3 + 0.2 * rng.normal(size=g.nelem), 0.0, 1.0)
+    res = optimize.simp(g, fill, active, frozen, fixed, {"a": F1, "b": F2}, {"a": 1.0, "b": 2.0},
+                        1.0, 0.3, 0.35, iters=16, r_mm=2.0, combine="worst", x0=x0,
+                        log=lambda *a: None)
+    restore()
+    np.savez_compressed(os.path.join(HERE, "simp_worst.npz"), shape=np.array(g.shape), fill=fill,
+                        active=active, frozen=frozen, fixed=fixed, F1=F1, F2=F2, x0=x0, vf=0.35,
+                        iters=16, x=res["x"], **_hist_arrays(res["history"]))
+
+
+def gen_config1(fem, optimize, iters=50):
+    """The 48x24x24 cantilever in FP64: E0=1, Emin=1e-9, nu=0.3, p=3 from iteration 1
+    (warm path with x0 = 0.3), no projection, r=1.5, vf=0.3, CG rtol 1e-8, 50 iterations."""
+    optimize.EMIN = 1e-9
+    restore = patch_simp_rtol(fem, 1e-8)
+    g, fixed, F = cantilever(fem, 48, 24, 24, edge_z=0.0)
+    active = np.ones(g.nelem, bool)
+    fill = np.ones(g.nelem)
+    frozen = np.zeros(g.nelem, bool)
+    logs = []
+    t0 = time.time()
+    res = optimize.simp(g, fill, active, frozen, fixed, {"c": F}, {"c": 1.0}, 1.0, 0.3, 0.3,
+                        iters=iters, r_mm=1.5, p_final=3.0, move=0.2, tol=0.0,
+                        x0=np.full(g.nelem, 0.3), beta_max=0.0, log=logs.append)
+    print(f"config1: {time.time() - t0:.0f} s")
+    np.savez_compressed(os.path.join(HERE, "simp_config1.npz"), shape=np.array(g.shape),
+                        fixed=fixed, F=F, iters=iters, x=res["x"], **_hist_arrays(res["history"]))
+    with open(os.path.join(HERE, "simp_config1_log.txt"), "w") as fh:
+        fh.write("\n".join(logs) + "\n")
+    optimize.EMIN = 1e-6
+    restore()
+
+
+def gen_validate(validate):
+    out = {}
+    for fn in validate.CHECKS:
+        name, ok, detail = fn()
+        out[fn.__name__] = {"name": name, "ok": bool(ok), "detail": detail}
+    ux, _ = validate._tension()
+    out["_tension_ux"] = float(ux)
+    ux_p, _ = validate._tension(fill_layer=0.4, nz=7)
+    out["_partial_ux"] = float(ux_p)
+    with open(os.path.join(HERE, "validate.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--skip-config1", action="store_true")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    fem, optimize, validate = install_stubs(a.ref)
+    jobs = {"ke": lambda: gen_ke(fem), "fem_small": lambda: gen_fem_small(fem),
+            "filter": lambda: gen_filter(optimize, fem),
+            "simp_small": lambda: gen_simp_small(fem, optimize),
+            "simp_small_tight": lambda: gen_simp_small(fem, optimize, rtol=1e-10),
+            "simp_worst": lambda: gen_simp_worst(fem, optimize),
+            "validate": lambda: gen_validate(validate)}
+    if not a.skip_config1:
+        jobs["config1"] = lambda: gen_config1(fem, optimize)
+    for name, fn in jobs.items():
+        if a.only and name not in a.only.split(","):
+            continue
+        t0 = time.time()
+        fn()
+        print(f"{name}: {time.time() - t0:.1f} s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,143 @@
+"""The GPU solve and SIMP loop against the reference's golden runs and the FP64 oracle.
+
+Parity bars: compliance within 1e-5 relative per solve; final density L-inf within 1e-3."""
+import numpy as np
+import pytest
+
+from anneal_gb300 import fem as G
+from anneal_gb300 import optimize as O
+from anneal_gb300 import problems as P
+from anneal_gb300 import validate as V
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid(shape):
+    return G.Grid(shape, 1.0, (0, 0, 0))
+
+
+@pytest.mark.parametrize("rtol", [1e-12, 1e-6])
+def test_solve_matches_reference(golden, rtol):
+    g = golden("fem_small.npz")
+    grid = _grid(tuple(int(s) for s in g["shape"]))
+    fem = G.FEM(grid, g["active"], g["fixed"], 0.3)
+    assert np.array_equal(fem.free, g["free"])
+    Fr = fem.reduce_load(g["F"])
+    u = fem.solve(fem.assemble(g["Ee_solve"]), [Fr], rtol=rtol)[0]
+    c = float(Fr @ u)
+    assert abs(c / float(g["compliance"]) - 1) < (1e-6 if rtol < 1e-7 else 1e-5)
+    assert fem.relres[-1] <= rtol * 1.0001
+    if rtol < 1e-7:
+        assert np.abs(u - g["u_sol"]).max() <= 1e-6 * np.abs(g["u_sol"]).max()
+    fem.close()
+
+
+def test_operator_matmul_on_reduced_vectors(golden):
+    g = golden("fem_small.npz")
+    grid = _grid(tuple(int(s) for s in g["shape"]))
+    fem = G.FEM(grid, g["active"], g["fixed"], 0.3)
+    y = fem.assemble(g["Ee"]) @ g["u_red"]
+    assert np.abs(y - g["y_red"]).max() <= 1e-6 * np.abs(g["y_red"]).max()
+    fem.close()
+
+
+def test_validation_gate_v1_to_v5():
+    for fn in (V.check_rigid_body, V.check_tension, V.check_cantilever, V.check_partial_volume,
+               V.check_determinism):
+        name, ok, detail = fn()
+        assert ok, f"{name}: {detail}"
+
+
+def test_unsupported_part_raises_solver_error():
+    """No fixed DOF: K is singular; the reference raises SolverError (fem.py:225-229)."""
+    w = P.cantilever(8, 4, 4)
+    fem = G.FEM(_grid(w.shape), w.active, np.zeros(0, int), 0.3)
+    with pytest.raises(G.SolverError, match="did not converge"):
+        fem.solve(fem.assemble(np.ones(w.nelem)), [fem.reduce_load(w.loads["c"])], rtol=1e-6, maxiter=200)
+    fem.close()
+
+
+def test_nonfinite_load_raises_solver_error():
+    w = P.cantilever(8, 4, 4)
+    fem = G.FEM(_grid(w.shape), w.active, w.fixed, 0.3)
+    F = fem.reduce_load(w.loads["c"]).copy()
+    F[len(F) // 2] = np.nan
+    with pytest.raises(G.SolverError):
+        fem.solve(fem.assemble(np.ones(w.nelem)), [F], rtol=1e-6, maxiter=200)
+    fem.close()
+
+
+def _simp_fixture(s, **kw):
+    grid = _grid(tuple(int(v) for v in s["shape"]))
+    return O.simp(grid, s["fill"], s["active"], s["frozen"], s["fixed"], {"down": s["F"]}, {"down": 1.0},
+                  float(s["E0"]), float(s["nu"]), float(s["vf"]), iters=int(s["iters"]), log=lambda *a: None,
+                  rtol=float(s["rtol"]), **kw)
+
+
+def test_simp_default_path_matches_reference(golden):
+    """Penalty ramp, projection continuation, frozen and partial-fill voxels (24 iterations)."""
+    s = golden("simp_small_tight.npz")
+    r = _simp_fixture(s)
+    c = np.array([h["compliance"][0] for h in r["history"]])
+    assert np.abs(c / s["h_compliance"][:, 0] - 1).max() < 1e-5
+    assert np.abs(r["x"] - s["x"]).max() < 1e-3
+    for k in ("p", "beta"):
+        assert np.array_equal(np.array([h[k] for h in r["history"]]), s[f"h_{k}"])
+    vol = np.array([h["volumeFraction"] for h in r["history"]])
+    assert np.abs(vol - s["h_volumeFraction"]).max() < 1e-5
+
+
+def test_simp_stock_tolerance_fp32_path(golden):
+    """The reference's own CG tolerance (1e-6) on the FP32 solver."""
+    s = golden("simp_small.npz")
+    r = _simp_fixture(s)
+    c = np.array([h["compliance"][0] for h in r["history"]])
+    assert np.abs(c / s["h_compliance"][:, 0] - 1).max() < 1e-4
+    assert np.abs(r["x"] - s["x"]).max() < 1e-2
+
+
+def test_simp_worst_case_combine(golden):
+    s = golden("simp_worst.npz")
+    grid = _grid(tuple(int(v) for v in s["shape"]))
+    r = O.simp(grid, s["fill"], s["active"], s["frozen"], s["fixed"], {"a": s["F1"], "b": s["F2"]},
+               {"a": 1.0, "b": 2.0}, 1.0, 0.3, float(s["vf"]), iters=int(s["iters"]), r_mm=2.0,
+               combine="worst", x0=s["x0"], log=lambda *a: None, rtol=1e-10)
+    c = np.array([h["compliance"] for h in r["history"]])
+    assert np.abs(c / s["h_compliance"] - 1).max() < 1e-5
+    assert np.abs(r["x"] - s["x"]).max() < 1e-3
+
+
+def test_config1_cantilever_50_iterations(golden):
+    """48x24x24 cantilever, E_min 1e-9, p = 3, r = 1.5, vf = 0.3, CG rtol 1e-8, 50 iterations:
+    compliance of every iteration within 1e-5 and the final density within 1e-3 (L-inf) of
+    the reference's own run."""
+    s = golden("simp_config1.npz")
+    w = P.cantilever(48, 24, 24)
+    old = O.EMIN
+    O.EMIN = 1e-9
+    try:
+        r = O.simp(_grid(w.shape), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, 1.0, 0.3, 0.3,
+                   iters=50, r_mm=1.5, p_final=3.0, move=0.2, tol=0.0, x0=np.full(w.nelem, 0.3),
+                   beta_max=0.0, log=lambda *a: None, rtol=1e-8)
+    finally:
+        O.EMIN = old
+    c = np.array([h["compliance"][0] for h in r["history"]])
+    assert np.abs(c / s["h_compliance"][:, 0] - 1).max() < 1e-5
+    assert np.abs(r["x"] - s["x"]).max() < 1e-3
+
+
+def test_log_line_format_matches_reference(golden):
+    """The per-iteration line is parsed by the reference GUI (gui/server.py:38-40)."""
+    import os
+    import re
+    ref = open(os.path.join(os.path.dirname(__file__), "golden", "simp_small_tight_log.txt")).read().splitlines()
+    pat = re.compile(r"^  it +(\d+)  p ([\d.]+)  b (\d+)  obj (\S+)  vol ([\d.]+)  change ([\d.]+)  "
+                     r"grey ([\d.]+)  cg (\d+)( amg)?  ([\d.]+)s$")
+    s = golden("simp_small_tight.npz")
+    lines = []
+    grid = _grid(tuple(int(v) for v in s["shape"]))
+    O.simp(grid, s["fill"], s["active"], s["frozen"], s["fixed"], {"down": s["F"]}, {"down": 1.0},
+           float(s["E0"]), float(s["nu"]), float(s["vf"]), iters=3, log=lines.append, rtol=1e-6)
+    its = [l for l in lines if l.startswith("  it ")]
+    assert len(its) == 3 and all(pat.match(l) for l in its)
+    assert all(pat.match(l) for l in ref if l.startswith("  it "))
