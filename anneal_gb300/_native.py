@@ -28,7 +28,8 @@ EXPORTS = [
     "anl_version", "anl_last_error", "anl_ctx_create", "anl_ctx_destroy", "anl_set_domain",
     "anl_free_mask", "anl_apply_K", "anl_solve", "anl_dot", "anl_element_energy",
     "anl_sensitivity", "anl_stiffness_scale", "anl_filter_init", "anl_filter_fwd",
-    "anl_filter_bwd", "anl_physical", "anl_oc_update", "anl_design_stats",
+    "anl_filter_bwd", "anl_physical", "anl_oc_update", "anl_design_stats", "anl_profile_apply",
+    "anl_launch_count",
 ]
 
 
@@ -66,6 +67,8 @@ _SIGS = {
     "anl_physical": (I, [P, P, P, D, D, P, P, P]),
     "anl_oc_update": (I, [P, P, P, P, P, P, D, D, D, D, P, ctypes.POINTER(I), ctypes.POINTER(D), P]),
     "anl_design_stats": (I, [P, P, P, P, P, P, ctypes.POINTER(D), P]),
+    "anl_profile_apply": (I, [P, P, P, I, ctypes.POINTER(D), P]),
+    "anl_launch_count": (I64, []),
 }
 
 

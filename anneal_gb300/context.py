@@ -111,6 +111,16 @@ class Context:
             N.check(st, "anl_solve")
         return st, list(iters), list(relres)
 
+    def profile_apply(self, u, y, reps):
+        """Mean milliseconds per launch of the level-0 K u kernel (element scales from the
+        last apply_K / solve)."""
+        _chk(u, self.vdtype, self.ndof, "u")
+        _chk(y, self.vdtype, self.ndof, "y")
+        ms = ctypes.c_double(0.0)
+        N.check(self.lib.anl_profile_apply(self._h, _p(u), _p(y), int(reps), ctypes.byref(ms), _stream()),
+                "anl_profile_apply")
+        return float(ms.value)
+
     def dot(self, a, b):
         _chk(a, _F64, self.ndof, "a")
         _chk(b, _F64, self.ndof, "b")

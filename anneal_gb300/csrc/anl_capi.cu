@@ -1,6 +1,7 @@
 // anl_capi.cu -- the extern "C" entry points declared in include/anneal_gb300.h, the
 // context life cycle and the host-side element matrix.
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 #include <new>
@@ -11,6 +12,9 @@
 namespace anl {
 
 static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -120,6 +124,7 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
 int design_stats(anl_ctx* c, const float* xold, const float* xnew, const float* xphys, const float* phi,
                  const uint8_t* frozen, double* out, cudaStream_t s);
 int ku_grid_blocks(const Dims& d);
+int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* ms, cudaStream_t s);
 
 // ------------------------------------------------------------------ context
 
@@ -299,6 +304,8 @@ int anl_version(void) { return 100; }
 
 const char* anl_last_error(void) { return anl::g_err; }
 
+int64_t anl_launch_count(void) { return (int64_t)anl::g_launches.load(); }
+
 int anl_ctx_create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, int flags) {
     anl::g_err[0] = 0;
     return create(out, nx, ny, nz, h, nu, flags);
@@ -411,6 +418,15 @@ int anl_oc_update(anl_ctx* ctx, const float* x, const float* dcx, const float* d
     NEED(ctx && x && dcx && dvx && phi && frozen && xnew, "anl_oc_update: null argument");
     NEED_FILTER("anl_oc_update");
     return oc_update(ctx, x, dcx, dvx, phi, frozen, move, beta, eta, vtarget, xnew, steps_h, lambda_h, S(stream));
+}
+
+int anl_profile_apply(anl_ctx* ctx, const void* u, void* y, int reps, double* ms_h, anl_stream_t stream) {
+    NEED(ctx && u && y && ms_h && reps >= 1, "anl_profile_apply: bad argument");
+    if (!ctx->domain_set) {
+        set_error("anl_profile_apply: call anl_set_domain first");
+        return ANL_ERR_STATE;
+    }
+    return solver_profile_apply(ctx, u, y, reps, ms_h, S(stream));
 }
 
 int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const float* xphys, const float* phi,

@@ -27,8 +27,11 @@ namespace anl {
         }                                                                                  \
     } while (0)
 
+// Every kernel launch of the library is followed by exactly one ANL_LAUNCH_CHECK, which
+// also counts it (anl_launch_count).
 #define ANL_LAUNCH_CHECK()                                                                 \
     do {                                                                                   \
+        anl::count_launch();                                                               \
         cudaError_t _e = cudaGetLastError();                                               \
         if (_e != cudaSuccess) {                                                           \
             anl::set_error("%s:%d launch: %s", __FILE__, __LINE__, cudaGetErrorString(_e)); \
@@ -43,6 +46,7 @@ namespace anl {
     } while (0)
 
 void set_error(const char* fmt, ...);
+void count_launch();
 
 // ------------------------------------------------------------------ grid
 
@@ -95,10 +99,11 @@ struct RedScratch {
 constexpr int kMaxRedVals = 8;
 constexpr int kRedBlocks = 1216;  // 152 SMs x 8: grid of the grid-stride vector kernels
 
-// Sum of `val` over the block, for NV values; result valid in thread 0.
+// Sum of `val` over the block, for NV values; result valid in the thread with flat index 0.
+// `tid` is the flat thread index (threadIdx.x for 1D blocks).
 template <int NV, int NT>
-__device__ __forceinline__ void block_sum(double (&val)[NV], double* smem /* NV*NT/32 */) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__device__ __forceinline__ void block_sum(double (&val)[NV], double* smem /* NV*NT/32 */, int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
         double s = val[v];
@@ -107,7 +112,7 @@ __device__ __forceinline__ void block_sum(double (&val)[NV], double* smem /* NV*
         if (lane == 0) smem[v * (NT / 32) + warp] = s;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             double s = 0;
@@ -122,9 +127,9 @@ __device__ __forceinline__ void block_sum(double (&val)[NV], double* smem /* NV*
 // block_sum. Returns true in the block (thread 0) that wrote the result.
 template <int NV>
 __device__ __forceinline__ bool finish_reduction(const double (&val)[NV], int bid, int nblocks,
-                                                 double* partials, unsigned* counter, double* out) {
+                                                 double* partials, unsigned* counter, double* out, int tid) {
     __shared__ bool last;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) partials[(int64_t)bid * NV + v] = val[v];
         __threadfence();
@@ -134,7 +139,7 @@ __device__ __forceinline__ bool finish_reduction(const double (&val)[NV], int bi
     __syncthreads();
     if (!last) return false;
     __threadfence();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         for (int v = 0; v < NV; ++v) {
             double s = 0;
             for (int b = 0; b < nblocks; ++b) s += ((volatile double*)partials)[(int64_t)b * NV + v];

@@ -127,9 +127,9 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
     if (MODE == F_OCVOL) {
         __shared__ double red[FT_N / 32];
         double v[1] = {vol};
-        block_sum<1, FT_N>(v, red);
+        block_sum<1, FT_N>(v, red, tid);
         const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        finish_reduction<1>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out);
+        finish_reduction<1>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out, tid);
     }
 }
 
@@ -352,8 +352,8 @@ __global__ void k_oc_scale(int64_t ne, const uint8_t* active, const uint8_t* fro
             v[1] += dvx[e];
             v[2] += 1.0;
         }
-    block_sum<3, DT>(v, sm);
-    finish_reduction<3>(v, blockIdx.x, gridDim.x, partials, counter, out);
+    block_sum<3, DT>(v, sm, threadIdx.x);
+    finish_reduction<3>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
 }
 
 // With no projection the volume is linear in xn: vol = sum_j wv_j xn_j + sum_frozen phi,
@@ -369,8 +369,8 @@ __global__ void k_oc_vol_linear(int64_t ne, const uint8_t* active, const uint8_t
             acc.add_prod(wv[e], xn);
         }
     double v[1] = {acc.value()};
-    block_sum<1, DT>(v, sm);
-    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out);
+    block_sum<1, DT>(v, sm, threadIdx.x);
+    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
 }
 
 __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,
@@ -382,8 +382,8 @@ __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* f
         v[e] = a && !fz ? phi[e] : 0.f;
         if (a && fz) f[0] += phi[e];
     }
-    block_sum<1, DT>(f, sm);
-    finish_reduction<1>(f, blockIdx.x, gridDim.x, partials, counter, out);
+    block_sum<1, DT>(f, sm, threadIdx.x);
+    finish_reduction<1>(f, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
 }
 
 __global__ void k_oc_final(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x, const float* dcx,
@@ -486,7 +486,7 @@ __global__ void k_stats(int64_t ne, const uint8_t* active, const uint8_t* frozen
     }
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
-    block_sum<3, DT>(v, sm);
+    block_sum<3, DT>(v, sm, threadIdx.x);
     if (threadIdx.x == 0) {
         for (int w = 0; w < DT / 32; ++w) mx = fmaxf(mx, smax[w]);
     }

@@ -114,8 +114,8 @@ __global__ void k_count_free(int64_t nn, const uint8_t* nmask, double* partials,
     double v[1] = {0.0};
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x)
         v[0] += (double)__popc(nmask[n] & 7);
-    block_sum<1, VT>(v, sm);
-    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out);
+    block_sum<1, VT>(v, sm, threadIdx.x);
+    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
 }
 
 __global__ void k_level0_E(int64_t ne, const float* escale, const uint8_t* active, float h, float* E) {
@@ -266,8 +266,8 @@ __global__ void k_dot_diag(int64_t nn, const T* v, const float* diag, double* pa
         for (int c = 0; c < 3; ++c) s.prod(v[3 * n + c] * dg, v[3 * n + c]);
     }
     double val[1] = {s.get()};
-    block_sum<1, VT>(val, sm);
-    finish_reduction<1>(val, blockIdx.x, gridDim.x, partials, counter, out);
+    block_sum<1, VT>(val, sm, threadIdx.x);
+    finish_reduction<1>(val, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
 }
 
 // ------------------------------------------------------------------ coarsest grid (FP64)
@@ -394,8 +394,8 @@ __global__ void k_dot_d(int64_t n, const double* a, const double* b, double* par
     double v[1] = {0.0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[0] = fma(a[i], b[i], v[0]);
-    block_sum<1, VT>(v, sm);
-    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out);
+    block_sum<1, VT>(v, sm, threadIdx.x);
+    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
 }
 
 // x (FP64) -> hi + lo in T
@@ -421,9 +421,9 @@ __global__ void k_true_resid(int64_t n, const double* b, const T* y1, const T* y
         r[i] = T(ri);
         v[0] = fma(ri, ri, v[0]);
     }
-    block_sum<1, VT>(v, sm);
+    block_sum<1, VT>(v, sm, threadIdx.x);
     __shared__ double res[1];
-    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res)) {
+    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x)) {
         if (threadIdx.x == 0) {
             sc->rr_true = res[0];
             if (set_state) {
@@ -465,9 +465,9 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
         if (!rs) b.prod(zi, q[i]);
     }
     double v[2] = {a.get(), b.get()};
-    block_sum<2, VT>(v, sm);
+    block_sum<2, VT>(v, sm, threadIdx.x);
     __shared__ double res[2];
-    if (finish_reduction<2>(v, blockIdx.x, gridDim.x, partials, counter, res)) {
+    if (finish_reduction<2>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x)) {
         if (threadIdx.x == 0) {
             const int it = sc->iters;
             sc->rz[it & 1] = res[0];
@@ -517,9 +517,9 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
         }
     }
     double v[1] = {rr.get()};
-    block_sum<1, VT>(v, sm);
+    block_sum<1, VT>(v, sm, threadIdx.x);
     __shared__ double res[1];
-    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res)) {
+    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x)) {
         if (threadIdx.x == 0) {
             sc->alpha = alpha;
             sc->rr = res[0];
@@ -750,7 +750,9 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
     const int64_t nn = L0.d.nn(), n = 3 * nn;
     int* restart = c->flag_d + 1;
     k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, f, L0.nmask, c->bbuf);
+    ANL_LAUNCH_CHECK();
     k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, x, L0.nmask, c->xbuf);
+    ANL_LAUNCH_CHECK();
     k_dot_d<<<vgrid(n), VT, 0, s>>>(n, c->bbuf, c->bbuf, c->partials, c->counter, c->red_out);
     ANL_LAUNCH_CHECK();
     k_init_scalars<<<1, 1, 0, s>>>(c->sc, rtol, maxiter, c->red_out);
@@ -777,6 +779,7 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
                 const T* z = (const T*)L0.x;
                 k_dots_rz_zq<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)L0.b, z, (const T*)c->q, c->sc, restart,
                                                          c->partials, c->counter);
+                ANL_LAUNCH_CHECK();
                 k_pupdate<T><<<vgrid(n), VT, 0, s>>>(n, z, (T*)c->p, c->sc, restart);
                 ANL_LAUNCH_CHECK();
                 ANL_TRY(apply_level<T>(c, L0, (const T*)c->p, (T*)c->q, s, &c->sc->pq, done));
@@ -832,6 +835,7 @@ int solver_setup_domain(anl_ctx* c, const uint8_t* active, const uint8_t* fixed,
         Level& F = c->lev[l - 1];
         Level& C = c->lev[l];
         k_eact_coarse<<<vgrid(C.d.ne()), VT, 0, s>>>(F.d, C.d, F.eact, C.eact);
+        ANL_LAUNCH_CHECK();
         k_mask_coarse<<<vgrid(C.d.nn()), VT, 0, s>>>(F.d, C.d, F.nmask, C.eact, C.nmask);
         ANL_LAUNCH_CHECK();
     }
@@ -883,6 +887,26 @@ int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, in
     if (worst == ANL_ERR_NONFINITE) set_error("a non-finite value appeared in CG");
     if (worst == ANL_ERR_BREAKDOWN) set_error("CG breakdown: the operator is not positive definite on the free DOFs");
     return worst;
+}
+
+int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* ms, cudaStream_t s) {
+    cudaEvent_t e0, e1;
+    ANL_CUDA(cudaEventCreate(&e0));
+    ANL_CUDA(cudaEventCreate(&e1));
+    ANL_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps; ++r) {
+        int st = c->fp64 ? apply_level<double>(c, c->lev[0], (const double*)u, (double*)y, s)
+                         : apply_level<float>(c, c->lev[0], (const float*)u, (float*)y, s);
+        if (st != ANL_OK) return st;
+    }
+    ANL_CUDA(cudaEventRecord(e1, s));
+    ANL_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    ANL_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = (double)t / reps;
+    return ANL_OK;
 }
 
 int solver_dot(anl_ctx* c, const double* a, const double* b, double* out, cudaStream_t s) {

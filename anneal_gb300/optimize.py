@@ -13,7 +13,7 @@ import numpy as np
 import torch
 
 from .context import Context, to_dev
-from .fem import FEM, FP32_RTOL_FLOOR
+from .fem import FEM
 
 EMIN = 1e-6       # optimize.py:18
 PNORM = 8.0       # optimize.py:19
@@ -58,124 +58,171 @@ def _continuation(it, iters, p_final, warm):
     return p_final if warm else min(p_final, 1.0 + 0.25 * ((it - 1) // hold))
 
 
+class SimpRunner:
+    """The device-resident state of one SIMP run and one ``step()`` per iteration.
+
+    ``simp`` drives it for the reference's interface; benchmarks and services that step
+    the loop themselves use it directly (``step_host`` exchanges the design with pinned
+    host memory around a step)."""
+
+    def __init__(self, grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=80, r_mm=None,
+                 p_final=3.0, move=0.2, combine="sum", log=print, x0=None, beta_max=BETA_MAX, rtol=None,
+                 maxiter=2000):
+        self.grid = grid
+        self.E0, self.vf, self.iters, self.p_final, self.move = float(E0), float(vf), int(iters), p_final, move
+        self.combine, self.log, self.beta_max, self.maxiter = combine, log, beta_max, maxiter
+        self.emin = EMIN
+        self.rtol = CG_RTOL if rtol is None else float(rtol)
+        self.fem = fem = FEM(grid, active, fixed, nu, log=log)
+        self.ctx = ctx = fem._ctx(fp64=False)
+        act = self.act = fem.act
+        ne = grid.nelem
+        fill = np.asarray(fill, float)
+        frozen = np.asarray(frozen, bool)
+        phi = fill[act]
+        frz = frozen[act]
+        des = ~frz
+        self.r_vox = max((r_mm or 1.5 * grid.h) / grid.h, 1.5)
+        ctx.filter_init(self.r_vox)
+        self.cases = list(loads)
+        mask = fem._mask_t.cpu().numpy()
+        F_host = np.stack([np.where(mask, np.asarray(loads[c], float), 0.0) for c in self.cases])
+        self.w = np.array([weights[c] for c in self.cases], float)
+        if all(np.allclose(f[fem.free], 0) for f in F_host):
+            raise ValueError("All loads are zero after mapping onto the grid. Check the load anchors' regions.")
+        # optimize.py:67-77
+        self.Vtot = phi.sum()
+        self.Vtarget = vf * self.Vtot
+        Vfrozen = phi[frz].sum()
+        x = np.ones(act.size)
+        x[des] = np.clip((self.Vtarget - Vfrozen) / max(phi[des].sum(), 1e-12), 0.01, 1.0)
+        self.warm = x0 is not None
+        if self.warm:
+            xs = np.clip(np.asarray(x0, float)[act], 0.0, 1.0)
+            cur = (phi[des] * xs[des]).sum()
+            if cur > 0:
+                x[des] = np.clip(xs[des] * (self.Vtarget - Vfrozen) / cur, 0.001, 1.0)
+
+        def full(v_act):
+            f = np.zeros(ne)
+            f[act] = v_act
+            return f
+
+        f32 = torch.float32
+        self.phi_t = to_dev(full(phi), f32)
+        self.frz_t = to_dev(full(frz).astype(np.uint8), torch.uint8)
+        self.x_t = to_dev(full(x), f32)
+        self.xnew_t = torch.empty_like(self.x_t)
+        self.xphys_t = torch.empty_like(self.x_t)
+        self.dxp_t = torch.empty_like(self.x_t)
+        self.escale_t = torch.empty_like(self.x_t)
+        self.dc_t = torch.empty_like(self.x_t)
+        self.dcx_t = torch.empty_like(self.x_t)
+        self.dv_t = torch.empty_like(self.x_t)
+        self.dvx_t = torch.empty_like(self.x_t)
+        self.F_t = to_dev(F_host, torch.float64)
+        self.U_t = torch.zeros_like(self.F_t)
+        self.beta = beta_max / 2 if self.warm else 0.0
+        self.beta_step = max(5, int(0.12 * iters))
+        self.beta_since = 0
+        self.c0 = None
+        self.base_iters = None
+        self.it = 0
+        self.hist = []
+        self.p = 1.0
+
+    def step(self):
+        """One SIMP iteration (optimize.py:105-172); returns its history record."""
+        t0 = time.time()
+        ctx, fem = self.ctx, self.fem
+        self.it += 1
+        it = self.it
+        p = self.p = _continuation(it, self.iters, self.p_final, self.warm)
+        if p >= self.p_final and not self.warm and self.beta_max > 0:   # optimize.py:111-116
+            if self.beta == 0:
+                self.beta, self.beta_since = 1.0, 0
+            elif self.beta_since >= self.beta_step and self.beta < self.beta_max:
+                self.beta, self.beta_since = min(self.beta_max, 2 * self.beta), 0
+            self.beta_since += 1
+        beta = self.beta
+        ctx.physical(self.x_t, self.frz_t, beta, ETA, self.xphys_t, self.dxp_t)
+        ctx.stiffness_scale(self.xphys_t, self.phi_t, self.E0, self.emin, p, self.escale_t)
+        last = fem.cg_iters[-1] if fem.cg_iters else None
+        rebuild = self.base_iters is None or (last is not None and last > 1.6 * self.base_iters)
+        fem.solve_device(self.escale_t, self.F_t, self.U_t, rtol=self.rtol, maxiter=self.maxiter, rebuild=rebuild)
+        if rebuild:
+            self.base_iters = fem.cg_iters[-1]
+        nc = len(self.cases)
+        cs = np.array([ctx.dot(self.F_t[c], self.U_t[c]) for c in range(nc)])
+        if self.c0 is None:
+            self.c0 = cs.copy()
+        if self.combine == "sum" or nc == 1:
+            obj = float(self.w @ cs)
+            coef = self.w
+        else:   # optimize.py:136-139
+            r = self.w * cs / self.c0
+            obj = float((r ** PNORM).sum() ** (1 / PNORM))
+            coef = (r / obj) ** (PNORM - 1) * self.w / self.c0
+        ctx.sensitivity(self.U_t, coef, self.xphys_t, self.dxp_t, self.phi_t, p, self.emin, self.E0, self.dc_t,
+                        self.dv_t)
+        ctx.filter_bwd(self.dc_t, self.dcx_t)
+        ctx.filter_bwd(self.dv_t, self.dvx_t)
+        ctx.oc_update(self.x_t, self.dcx_t, self.dvx_t, self.phi_t, self.frz_t, self.move, beta, ETA, self.Vtarget,
+                      self.xnew_t)
+        ctx.physical(self.xnew_t, self.frz_t, beta, ETA, self.xphys_t, None)
+        change, grey, vol, ndes = ctx.design_stats(self.x_t, self.xnew_t, self.xphys_t, self.phi_t, self.frz_t)
+        if ndes == 0:
+            change, grey = 0.0, 0.0
+        self.x_t, self.xnew_t = self.xnew_t, self.x_t
+        rec = {"iter": it, "objective": obj, "compliance": cs.tolist(), "p": p, "beta": beta,
+               "volumeFraction": float(vol / self.Vtot), "change": change, "grey": grey,
+               "cgIters": fem.cg_iters[-nc:], "amgRebuilt": bool(rebuild), "seconds": time.time() - t0}
+        self.hist.append(rec)
+        self.log(f"  it {it:3d}  p {p:.2f}  b {beta:.0f}  obj {obj:.4g}  vol {rec['volumeFraction']:.3f}  "
+                 f"change {change:.3f}  grey {grey:.2f}  cg {fem.cg_iters[-1]}{' amg' if rebuild else ''}  "
+                 f"{rec['seconds']:.1f}s")
+        return rec
+
+    def step_host(self, x_in, x_out):
+        """One iteration with the design exchanged through host memory: x_in (host float32,
+        full grid) is copied in, the updated design is copied to x_out (host float32)."""
+        self.x_t.copy_(x_in, non_blocking=True)
+        rec = self.step()
+        x_out.copy_(self.x_t, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return rec
+
+    def converged(self, tol):
+        rec = self.hist[-1]
+        return (rec["p"] >= self.p_final and rec["beta"] >= self.beta_max
+                and self.it > (5 if self.warm else 10) and rec["change"] < tol)
+
+    def result(self, t_start):
+        xout = np.zeros(self.grid.nelem)
+        xout[self.act] = self.xphys_t.cpu().numpy().astype(float)[self.act]
+        return {"x": xout, "history": self.hist, "fem_builds": self.fem.amg_builds, "rMM": self.r_vox * self.grid.h,
+                "seconds": time.time() - t_start, "cases": self.cases}
+
+    def close(self):
+        self.fem.close()
+
+
 def simp(grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf,
          iters=80, r_mm=None, p_final=3.0, move=0.2, combine="sum", log=print, tol=0.01, x0=None,
          beta_max=BETA_MAX, rtol=None, maxiter=2000):
     """optimize.py:50-180 on the GPU. ``rtol`` overrides the CG tolerance (default CG_RTOL,
     the reference's hard-coded 1e-6); the void stiffness is the module constant EMIN."""
     t_start = time.time()
-    emin = EMIN
-    rtol = CG_RTOL if rtol is None else float(rtol)
-    fem = FEM(grid, active, fixed, nu, log=log)
-    ctx = fem._ctx(fp64=False)
-    act = fem.act
-    ne = grid.nelem
-    fill = np.asarray(fill, float)
-    frozen = np.asarray(frozen, bool)
-    phi = fill[act]
-    frz = frozen[act]
-    des = ~frz
-    h = grid.h
-    r_vox = max((r_mm or 1.5 * h) / h, 1.5)
-    ctx.filter_init(r_vox)
-    cases = list(loads)
-    F_host = np.stack([np.where(fem._mask_t.cpu().numpy(), np.asarray(loads[c], float), 0.0) for c in cases])
-    w = np.array([weights[c] for c in cases], float)
-    if all(np.allclose(f[fem.free], 0) for f in F_host):
-        raise ValueError("All loads are zero after mapping onto the grid. Check the load anchors' regions.")
-
-    Vtot = phi.sum()
-    Vtarget = vf * Vtot
-    Vfrozen = phi[frz].sum()
-    x = np.ones(act.size)
-    x[des] = np.clip((Vtarget - Vfrozen) / max(phi[des].sum(), 1e-12), 0.01, 1.0)
-    warm = x0 is not None
-    if warm:
-        xs = np.clip(np.asarray(x0, float)[act], 0.0, 1.0)
-        cur = (phi[des] * xs[des]).sum()
-        if cur > 0:
-            x[des] = np.clip(xs[des] * (Vtarget - Vfrozen) / cur, 0.001, 1.0)
-
-    def full(v_act):
-        f = np.zeros(ne)
-        f[act] = v_act
-        return f
-
-    f32 = torch.float32
-    phi_t = to_dev(full(phi), f32)
-    frz_t = to_dev(full(frz).astype(np.uint8), torch.uint8)
-    x_t = to_dev(full(x), f32)
-    xnew_t = torch.empty_like(x_t)
-    xphys_t = torch.empty_like(x_t)
-    dxp_t = torch.empty_like(x_t)
-    escale_t = torch.empty_like(x_t)
-    dc_t = torch.empty_like(x_t)
-    dcx_t = torch.empty_like(x_t)
-    dv_t = torch.empty_like(x_t)
-    dvx_t = torch.empty_like(x_t)
-    F_t = to_dev(F_host, torch.float64)
-    U_t = torch.zeros_like(F_t)
-
-    beta = 0.0
-    hist = []
-    c0 = None
-    base_iters = None
-    p = 1.0
-    if warm:
-        beta = beta_max / 2
-    beta_step = max(5, int(0.12 * iters))
-    beta_since = 0
-    for it in range(1, iters + 1):
-        t0 = time.time()
-        p = _continuation(it, iters, p_final, warm)
-        if p >= p_final and not warm and beta_max > 0:   # optimize.py:111-116
-            if beta == 0:
-                beta, beta_since = 1.0, 0
-            elif beta_since >= beta_step and beta < beta_max:
-                beta, beta_since = min(beta_max, 2 * beta), 0
-            beta_since += 1
-        ctx.physical(x_t, frz_t, beta, ETA, xphys_t, dxp_t)
-        ctx.stiffness_scale(xphys_t, phi_t, E0, emin, p, escale_t)
-        last = fem.cg_iters[-1] if fem.cg_iters else None
-        rebuild = base_iters is None or (last is not None and last > 1.6 * base_iters)
-        fem.solve_device(escale_t, F_t, U_t, rtol=rtol, maxiter=maxiter, rebuild=rebuild)
-        if rebuild:
-            base_iters = fem.cg_iters[-1]
-        cs = np.array([ctx.dot(F_t[c], U_t[c]) for c in range(len(cases))])
-        if c0 is None:
-            c0 = cs.copy()
-        if combine == "sum" or len(cases) == 1:
-            obj = float(w @ cs)
-            coef = w
-        else:   # optimize.py:136-139
-            r = w * cs / c0
-            obj = float((r ** PNORM).sum() ** (1 / PNORM))
-            coef = (r / obj) ** (PNORM - 1) * w / c0
-        ctx.sensitivity(U_t, coef, xphys_t, dxp_t, phi_t, p, emin, E0, dc_t, dv_t)
-        ctx.filter_bwd(dc_t, dcx_t)
-        ctx.filter_bwd(dv_t, dvx_t)
-        ctx.oc_update(x_t, dcx_t, dvx_t, phi_t, frz_t, move, beta, ETA, Vtarget, xnew_t)
-        ctx.physical(xnew_t, frz_t, beta, ETA, xphys_t, None)
-        change, grey, vol, ndes = ctx.design_stats(x_t, xnew_t, xphys_t, phi_t, frz_t)
-        if ndes == 0:
-            change, grey = 0.0, 0.0
-        x_t, xnew_t = xnew_t, x_t
-        hist.append({"iter": it, "objective": obj, "compliance": cs.tolist(), "p": p, "beta": beta,
-                     "volumeFraction": float(vol / Vtot), "change": change,
-                     "grey": grey, "cgIters": fem.cg_iters[-len(cases):], "amgRebuilt": bool(rebuild),
-                     "seconds": time.time() - t0})
-        log(f"  it {it:3d}  p {p:.2f}  b {beta:.0f}  obj {obj:.4g}  vol {hist[-1]['volumeFraction']:.3f}  "
-            f"change {change:.3f}  grey {grey:.2f}  cg {fem.cg_iters[-1]}{' amg' if rebuild else ''}  "
-            f"{hist[-1]['seconds']:.1f}s")
-        if p >= p_final and beta >= beta_max and it > (5 if warm else 10) and change < tol:
-            log(f"  converged at iteration {it}")
+    run = SimpRunner(grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=iters, r_mm=r_mm,
+                     p_final=p_final, move=move, combine=combine, log=log, x0=x0, beta_max=beta_max, rtol=rtol,
+                     maxiter=maxiter)
+    for _ in range(iters):
+        run.step()
+        if run.converged(tol):
+            log(f"  converged at iteration {run.it}")
             break
-
-    xout = np.zeros(ne)
-    xout[act] = xphys_t.cpu().numpy().astype(float)[act]
-    res = {"x": xout, "history": hist, "fem_builds": fem.amg_builds, "rMM": r_vox * h,
-           "seconds": time.time() - t_start, "cases": cases}
-    fem.close()
+    res = run.result(t_start)
+    run.close()
     return res
 
 

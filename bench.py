@@ -1,0 +1,317 @@
+"""SIMP iterations per second on the 256x128x128 L-bracket (12.8M DOF), one GB300.
+
+A step is one SIMP iteration of the GPU loop (filter + projection, stiffness scale,
+multigrid-preconditioned CG to relative residual 1e-6 warm-started from the previous
+displacement, sensitivity, two filter backward passes, OC bisection, history values).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs under torchrun with one independent replica per GPU (the solve has no
+cross-GPU exchange): value = total iterations / max rank time. ``--impl reference`` times
+the FP64 CPU oracle (the restatement of the reference's solver) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SIMP iters/s at 12.8M DOF; learned vs plain GPU PCG at rel. residual 1e-6"
+UNIT = "iter/s"
+SCALE = 4.0 / 3.0          # 256 x 128 x 128 voxels
+RTOL = 1e-6
+
+
+def workload_config():
+    return {"workload": "lbracket-256x128x128", "dofs": 3 * 257 * 129 * 129, "elements": 256 * 128 * 128,
+            "penalty": 3.0, "filter_r": 2.0, "vf": 0.25, "emin": 1e-9, "rtol": RTOL,
+            "warm_start": "previous-iterate displacement", "l2": "flushed (512 MB write) between timed steps"}
+
+
+def make_workload():
+    from anneal_gb300 import problems as P
+    return P.lbracket(scale=SCALE, vf=0.25, r_vox=2.0, emin=1e-9)
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per K u launch from the committed ncu summary, if there is one."""
+    path = os.path.join(ROOT, "profiles", "ku_apply_256x128x128.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of the SM clock during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+        return False
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        rows = []
+        for line in getattr(self, "out", "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                rows.append((float(f[0]), float(f[1]), f[3:7]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "reasons": reasons}
+
+
+# ------------------------------------------------------------------ CPU oracle sample
+
+def cpu_sample(w, n_cg, cg_sample=3):
+    """One SIMP iteration of the FP64 oracle at full size, with the CG cut to `cg_sample`
+    iterations and its per-iteration time scaled to `n_cg` (the GPU run's mean CG count).
+    Returns (seconds per SIMP iteration, threads, description)."""
+    from oracle import oracle as O
+    O.build()
+    t_all = time.perf_counter()
+    fem = O.OracleFEM(w.shape, w.h, w.active, w.fixed, w.nu)
+    filt = O.OracleFilter(w.shape, w.active, w.r_vox)
+    act = fem.act
+    phi = w.fill[act]
+    frz = w.frozen[act]
+    x = np.full(act.size, w.vf)
+    x[frz] = 1.0
+    t0 = time.perf_counter()
+    xp = filt.forward(x)
+    xp[frz] = 1.0
+    Ee = w.E0 * phi * (w.emin + xp ** 3 * (1 - w.emin))
+    F = np.where(fem.mask, w.loads["down"], 0.0)
+    t1 = time.perf_counter()
+    # the CG: setup + `cg_sample` iterations, then one more run of 1 iteration to separate
+    # the multigrid setup from the per-iteration cost
+    import ctypes
+    E = fem.full_E(Ee)
+    ts, u = [], None
+    for k in (1, cg_sample + 1):
+        u = np.zeros(3 * fem.nnode)
+        it, rr = ctypes.c_int(0), ctypes.c_double(0.0)
+        ta = time.perf_counter()
+        O.lib().orc_pcg(*fem.shape, O._p(fem.ke), O._p(E), O._p(fem.mask_u8, O._u8), O._p(F), O._p(u),
+                        1e-30, k, 1, 2, ctypes.byref(it), ctypes.byref(rr))
+        ts.append(time.perf_counter() - ta)
+    per_cg = (ts[1] - ts[0]) / cg_sample
+    setup = ts[0] - per_cg
+    t2 = time.perf_counter()
+    ce = fem.element_energy(u)
+    dc = -3 * xp ** 2 * (1 - w.emin) * w.E0 * phi * ce
+    dcx = filt.backward(np.minimum(dc, 0.0))
+    dvx = filt.backward(phi)
+    O.oc_update(filt, x, dcx, dvx, phi, frz, 0.2, 0.0, w.vf * phi.sum())
+    t3 = time.perf_counter()
+    per_iter = (t1 - t0) + setup + per_cg * n_cg + (t3 - t2)
+    desc = (f"one SIMP iteration of the FP64 oracle at 256x128x128: filter, stiffness, multigrid setup, "
+            f"{cg_sample} CG iterations scaled to {n_cg:.1f} (the GPU run's mean per solve), sensitivity, "
+            f"2 filter backward passes and the OC bisection; sample took {time.perf_counter() - t_all:.1f} s")
+    return per_iter, O.num_threads(), desc
+
+
+# ------------------------------------------------------------------ arms
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w = make_workload()
+    n_cg = float(os.environ.get("ANL_BENCH_CG_ITERS", "40"))
+    times = []
+    for s in range(args.warmup + args.steps):
+        t, threads, desc = cpu_sample(w, n_cg)
+        if s >= args.warmup:
+            times.append(t)
+    tmean = float(np.mean(times))
+    value = 1.0 / tmean
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmean, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from anneal_gb300 import _native as N
+    from anneal_gb300 import optimize as OPT
+    from anneal_gb300.fem import Grid
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = make_workload()
+    grid = Grid(w.shape, w.h, (0, 0, 0))
+    OPT.EMIN = w.emin
+    run = OPT.SimpRunner(grid, w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, w.E0, w.nu, w.vf,
+                         iters=10 ** 6, r_mm=w.r_vox, p_final=3.0, move=0.2, x0=np.full(w.nelem, w.vf),
+                         beta_max=0.0, rtol=RTOL, log=lambda *a: None)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        run.step()
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    barrier()
+    lib = N.load()
+    launches0 = lib.anl_launch_count()
+    cg0 = len(run.fem.cg_iters)
+    total_ms = 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run.step()
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+    barrier()
+    launches = lib.anl_launch_count() - launches0
+    cg_counts = run.fem.cg_iters[cg0:]
+    t_max = total_ms
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * args.steps / (t_max / 1e3)
+
+    # end to end: the design goes host -> device -> host around every step (pinned buffers)
+    x_in = torch.empty(w.nelem, dtype=torch.float32).pin_memory()
+    x_out = torch.empty_like(x_in).pin_memory()
+    x_in.copy_(run.x_t.cpu())
+    e2e_ms = 0.0
+    barrier()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run.step_host(x_in, x_out)
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        x_in.copy_(x_out)
+    barrier()
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    e2e = world * args.steps / (e2e_ms / 1e3)
+
+    # dominant kernel: the fine-level K u, timed alone with CUDA events on this stream
+    ctx = run.ctx
+    u = torch.randn(ctx.ndof, dtype=torch.float32, device="cuda") * run.fem._mask_t.float()
+    y = torch.empty_like(u)
+    ctx.apply_K(run.escale_t, u, y)
+    ms = ctx.profile_apply(u, y, 20)
+    nn, ne = ctx.nn, ctx.ne
+    alg_bytes = 24 * nn + 4 * ne
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    peak, peak_kind = read_peaks()
+    traffic = profile_traffic()
+    flops = 1152.0 * ne
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (FP64 CG scalars and solution)",
+                "data": "synthetic", "config": dict(workload_config(), parallelism=f"replicas x{world}"),
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * w.nelem,
+                        "d2h_bytes_per_step": 4 * w.nelem},
+                "gpu_launches": int(launches),
+                "cg_iters_per_solve": float(np.mean(cg_counts)) if cg_counts else None,
+                "roofline": {"kernel": "ku_kernel<float,APPLY> (fine-level K u)", "bound": "hbm",
+                             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
+                             "ms_per_launch": ms, "fp32_tflops": flops / (ms * 1e-3) / 1e12},
+                "clocks": clk.summary()}
+        if world == 1 and not args.no_cpu_baseline:
+            n_cg = float(np.mean(cg_counts)) if cg_counts else 40.0
+            t, threads, desc = cpu_sample(w, n_cg)
+            line["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": desc}
+        print(json.dumps(line), flush=True)
+    run.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

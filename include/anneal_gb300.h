@@ -133,6 +133,18 @@ int anl_oc_update(anl_ctx* ctx, const float* x, const float* dcx, const float* d
 int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const float* xphys,
                      const float* phi, const uint8_t* frozen, double* out_h, anl_stream_t stream);
 
+/* ---------------------------------------------------------------- measurement */
+
+/* Number of kernels this library has launched in the process so far (no counterpart in
+   the reference; lets a benchmark count the GPU launches inside its timed region). */
+int64_t anl_launch_count(void);
+
+/* Benchmark hook (no counterpart in the reference): launches the level-0 K u kernel
+   `reps` times on `stream` between two CUDA events and writes the mean time per launch in
+   milliseconds to *ms_h. The element scales are those of the last anl_apply_K / anl_solve
+   on this context; u must be zero on non-free DOFs (context precision). */
+int anl_profile_apply(anl_ctx* ctx, const void* u, void* y, int reps, double* ms_h, anl_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
