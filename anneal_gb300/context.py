@@ -98,7 +98,8 @@ class Context:
 
     def solve(self, escale, F, X, rtol, maxiter=2000, rebuild=True):
         """F, X: (nrhs, ndof) float64; X holds the initial guesses. Returns (status, iters,
-        relres) without raising on MAXITER / NONFINITE / BREAKDOWN (the caller decides)."""
+        relres) without raising on MAXITER / NONFINITE / BREAKDOWN / SINGULAR (the caller
+        decides: each means the part is not properly supported or the solve failed)."""
         _chk(escale, _F32, self.ne, "escale")
         nrhs = F.shape[0] if F.dim() == 2 else 1
         _chk(F, _F64, nrhs * self.ndof, "F")
@@ -107,7 +108,8 @@ class Context:
         relres = (ctypes.c_double * nrhs)()
         st = self.lib.anl_solve(self._h, _p(escale), _p(F), _p(X), nrhs, float(rtol), int(maxiter),
                                 1 if rebuild else 0, iters, relres, _stream())
-        if st not in (N.ANL_OK, N.ANL_ERR_MAXITER, N.ANL_ERR_NONFINITE, N.ANL_ERR_BREAKDOWN):
+        if st not in (N.ANL_OK, N.ANL_ERR_MAXITER, N.ANL_ERR_NONFINITE, N.ANL_ERR_BREAKDOWN,
+                      N.ANL_ERR_SINGULAR):
             N.check(st, "anl_solve")
         return st, list(iters), list(relres)
 

@@ -32,4 +32,21 @@ struct KuArgs {
 template <class T>
 int launch_ku(int mode, const KuArgs<T>& a, const KeBlocks<T>& kb, cudaStream_t s);
 
+// r = b - K32 x with x = xhi + xlo, evaluated in float-pair arithmetic; ||r||^2 -> *rr_out
+struct ResidHpArgs {
+    Dims d;
+    int kz = 0;
+    const float* E = nullptr;
+    const uint8_t* nmask = nullptr;
+    const float* xhi = nullptr;
+    const float* xlo = nullptr;
+    const double* b = nullptr;
+    float* r = nullptr;
+    double* partials = nullptr;
+    unsigned* counter = nullptr;
+    int partial_capacity = 0;
+    double* rr_out = nullptr;
+};
+int launch_resid_hp(const ResidHpArgs& a, const KeBlocks<float>& kb, cudaStream_t s);
+
 }  // namespace anl

@@ -214,6 +214,171 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeBlocks<T>& kb, cudaStream
     return ANL_OK;
 }
 
+
+// ------------------------------------------------------------------ accurate residual
+//
+// r = b - K32 x for x held in FP64 (as the pair x_hi + x_lo of floats), where K32 is the
+// FP32 operator above (the element blocks rounded to FP32). Differences, products and sums
+// are carried as unevaluated float pairs (TwoSum / TwoProd), so the result is accurate to
+// about eps^2 of the summed terms: the FP32 CG can certify ||b - K32 x|| <= rtol ||b||
+// far below the FP32 rounding floor of a plain evaluation (eps |K| |x|), at a fraction of
+// the cost of FP64 arithmetic on this part.
+
+struct F2 {
+    float s, c;
+};
+
+__device__ __forceinline__ void f2_add(F2& a, float p) {
+    float t, e;
+    two_sum(a.s, p, t, e);
+    a.s = t;
+    a.c += e;
+}
+
+__global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, KeBlocks<float> kb) {
+    __shared__ float sh[3][KU_HY][KU_HX][3];
+    __shared__ float sl[3][KU_HY][KU_HX][3];
+    __shared__ float sE[2][KU_EY][KU_EX];
+    __shared__ double sred[KU_NT / 32];
+    const Dims d = a.d;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * KU_BX + tx;
+    const int i0 = blockIdx.x * KU_BX, j0 = blockIdx.y * KU_BY, k0 = blockIdx.z * a.kz;
+    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+
+    auto load_nodes = [&](int slot, int kk) {
+        const bool kin = kk >= 0 && kk < NZn;
+        for (int f = tid; f < KU_HY * KU_HX * 3; f += KU_NT) {
+            const int row = f / (KU_HX * 3);
+            const int w = f - row * (KU_HX * 3);
+            const int c = w / 3, comp = w - 3 * c;
+            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
+            float vh = 0.f, vl = 0.f;
+            if (kin && gi >= 0 && gi < NXn && gj >= 0 && gj < NYn) {
+                const int64_t g = 3 * d.node(gi, gj, kk) + comp;
+                vh = a.xhi[g];
+                vl = a.xlo[g];
+            }
+            sh[slot][row][c][comp] = vh;
+            sl[slot][row][c][comp] = vl;
+        }
+    };
+    auto load_elems = [&](int slot, int ke) {
+        const bool kin = ke >= 0 && ke < d.nz;
+        for (int f = tid; f < KU_EY * KU_EX; f += KU_NT) {
+            const int row = f / KU_EX, c = f - row * KU_EX;
+            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
+            float v = 0.f;
+            if (kin && gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny) v = a.E[d.elem(gi, gj, ke)];
+            sE[slot][row][c] = v;
+        }
+    };
+
+    load_nodes(0, k0 - 1);
+    load_nodes(1, k0);
+    load_elems(0, k0 - 1);
+    double rr = 0.0;
+    const int i = i0 + tx, j = j0 + ty;
+    const int kend = min(k0 + a.kz, NZn);
+    for (int k = k0; k < kend; ++k) {
+        const int r = k - k0;
+        const int sl3[3] = {r % 3, (r + 1) % 3, (r + 2) % 3};
+        const int e_lo = r & 1, e_hi = (r + 1) & 1;
+        load_nodes(sl3[2], k + 1);
+        load_elems(e_hi, k);
+        __syncthreads();
+        if (i < NXn && j < NYn) {
+            float uh[3], ul[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                uh[c] = sh[sl3[1]][ty + 1][tx + 1][c];
+                ul[c] = sl[sl3[1]][ty + 1][tx + 1][c];
+            }
+            F2 y[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 1
+            for (int oct = 0; oct < 8; ++oct) {
+                const int sx = (oct & 1) ? 1 : -1, sy = (oct & 2) ? 1 : -1, sz = (oct & 4) ? 1 : -1;
+                const float Eo = sE[sz > 0 ? e_hi : e_lo][ty + (sy > 0 ? 1 : 0)][tx + (sx > 0 ? 1 : 0)];
+                if (Eo == 0.f) continue;
+                F2 w[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+                for (int dlt = 1; dlt < 8; ++dlt) {
+                    const int mx = sx * (dlt & 1), my = sy * ((dlt >> 1) & 1), mz = sz * ((dlt >> 2) & 1);
+                    const int slot = sl3[mz + 1];
+                    float th[3], tc[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float sg = c == 0 ? (float)sx : (c == 1 ? (float)sy : (float)sz);
+                        float dh, de;
+                        two_sum(sh[slot][ty + 1 + my][tx + 1 + mx][c], -uh[c], dh, de);
+                        const float dl = sl[slot][ty + 1 + my][tx + 1 + mx][c] - ul[c];
+                        th[c] = sg * dh;
+                        tc[c] = sg * (de + dl);
+                    }
+                    const float* B = kb.blk[dlt];
+#pragma unroll
+                    for (int rr3 = 0; rr3 < 3; ++rr3)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            float p, e;
+                            two_prod(B[3 * rr3 + c], th[c], p, e);
+                            f2_add(w[rr3], p);
+                            w[rr3].c += e + B[3 * rr3 + c] * tc[c];
+                        }
+                }
+#pragma unroll
+                for (int rr3 = 0; rr3 < 3; ++rr3) {
+                    const float sg = rr3 == 0 ? (float)sx : (rr3 == 1 ? (float)sy : (float)sz);
+                    float p, e;
+                    two_prod(sg * Eo, w[rr3].s, p, e);
+                    f2_add(y[rr3], p);
+                    y[rr3].c += e + sg * Eo * w[rr3].c;
+                }
+            }
+            const int64_t n = d.node(i, j, k);
+            const uint8_t nm = a.nmask[n];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                double rc = 0.0;
+                if ((nm >> c) & 1) rc = a.b[3 * n + c] - ((double)y[c].s + (double)y[c].c);
+                a.r[3 * n + c] = (float)rc;
+                rr = fma(rc, rc, rr);
+            }
+        }
+        __syncthreads();
+    }
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rr += __shfl_down_sync(0xffffffffu, rr, o);
+    if (lane == 0) sred[warp] = rr;
+    __syncthreads();
+    double v[1] = {0.0};
+    if (tid == 0)
+        for (int w = 0; w < KU_NT / 32; ++w) v[0] += sred[w];
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    __shared__ double res[1];
+    if (finish_reduction<1>(v, bid, nb, a.partials, a.counter, res, tid)) {
+        if (tid == 0) *a.rr_out = res[0];
+    }
+}
+
+int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, cudaStream_t s) {
+    ResidHpArgs a = args;
+    const Dims& d = a.d;
+    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+    const int chunks = ceil_div(NZn, 16);
+    a.kz = ceil_div(NZn, chunks);
+    dim3 grid(ceil_div(NXn, KU_BX), ceil_div(NYn, KU_BY), ceil_div(NZn, a.kz));
+    if ((int64_t)grid.x * grid.y * grid.z > a.partial_capacity) {
+        set_error("accurate residual: %d blocks exceed the reduction scratch (%d)", grid.x * grid.y * grid.z,
+                  a.partial_capacity);
+        return ANL_ERR_BADARG;
+    }
+    ku_resid_hp_kernel<<<grid, dim3(KU_BX, KU_BY), 0, s>>>(a, kb);
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
 int ku_grid_blocks(const Dims& d) {
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
     const int chunks = ceil_div(NZn, 16);

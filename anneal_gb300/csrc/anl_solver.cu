@@ -309,11 +309,19 @@ __global__ void k_assemble_dense(Dims d, const float* E, const uint8_t* nmask, c
 
 // In-place lower Cholesky factor of the n x n SPD matrix A (one CTA, right-looking).
 __global__ void __launch_bounds__(1024) k_cholesky(double* A, int n, int* flag) {
-    __shared__ double piv;
+    __shared__ double piv, dmax;
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int j = 0; j < n; ++j) m = fmax(m, A[(int64_t)j * n + j]);
+        dmax = m;
+    }
+    __syncthreads();
     for (int j = 0; j < n; ++j) {
         if (threadIdx.x == 0) {
             const double a = A[(int64_t)j * n + j];
-            if (!(a > 0.0)) {
+            // a pivot this small relative to the largest diagonal means the coarse problem
+            // has a floating (rigid-body) mode: treat it as singular
+            if (!(a > 1e-12 * dmax)) {
                 *flag = 1;
                 piv = 1.0;
             } else {
@@ -721,7 +729,22 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     return ANL_OK;
 }
 
-// r = b - K x with x (FP64, ctx->xbuf) split into hi + lo; updates the CG state.
+// r = b - K x with x in FP64 (ctx->xbuf): the FP64 operator in FP64 mode; in FP32 mode the
+// FP32 operator evaluated in float-pair arithmetic on x = hi + lo. Updates the CG state.
+__global__ void k_resid_state(PcgScalars* sc, const double* rr, int set_state) {
+    const double v = *rr;
+    sc->rr_true = v;
+    if (set_state) {
+        sc->rr = v;
+        if (!isfinite(v)) {
+            sc->done = 3;
+            sc->nonfinite = 1;
+        } else {
+            sc->done = v <= sc->tol2 ? 1 : 0;
+        }
+    }
+}
+
 template <class T>
 static int true_residual(anl_ctx* c, int set_state, cudaStream_t s) {
     Level& L0 = c->lev[0];
@@ -731,14 +754,25 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s) {
         ANL_TRY(apply_level<T>(c, L0, (const T*)(const void*)c->xbuf, (T*)c->y1, s));
         k_true_resid<T><<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (const T*)c->y1, nullptr, r, c->sc, set_state, c->partials,
                                                 c->counter);
-    } else {
-        k_split<T><<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (T*)c->xhi, (T*)c->xlo);
         ANL_LAUNCH_CHECK();
-        ANL_TRY(apply_level<T>(c, L0, (const T*)c->xhi, (T*)c->y1, s));
-        ANL_TRY(apply_level<T>(c, L0, (const T*)c->xlo, (T*)c->y2, s));
-        k_true_resid<T><<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (const T*)c->y1, (const T*)c->y2, r, c->sc, set_state,
-                                                c->partials, c->counter);
+        return ANL_OK;
     }
+    k_split<float><<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (float*)c->xhi, (float*)c->xlo);
+    ANL_LAUNCH_CHECK();
+    ResidHpArgs a;
+    a.d = L0.d;
+    a.E = L0.E;
+    a.nmask = L0.nmask;
+    a.xhi = (const float*)c->xhi;
+    a.xlo = (const float*)c->xlo;
+    a.b = c->bbuf;
+    a.r = (float*)(void*)r;
+    a.partials = c->partials;
+    a.counter = c->counter;
+    a.partial_capacity = c->part_cap;
+    a.rr_out = c->red_out + 8;
+    ANL_TRY(launch_resid_hp(a, c->kbf, s));
+    k_resid_state<<<1, 1, 0, s>>>(c->sc, c->red_out + 8, set_state);
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }
