@@ -123,6 +123,14 @@ class Context:
                 "anl_profile_apply")
         return float(ms.value)
 
+    def mg_info(self):
+        """[(element dims, lambda_max estimate)] per multigrid level."""
+        nlev = ctypes.c_int(0)
+        dims = (ctypes.c_int * 48)()
+        lmax = (ctypes.c_double * 16)()
+        N.check(self.lib.anl_mg_info(self._h, ctypes.byref(nlev), dims, lmax), "anl_mg_info")
+        return [((dims[3 * l], dims[3 * l + 1], dims[3 * l + 2]), lmax[l]) for l in range(nlev.value)]
+
     def dot(self, a, b):
         _chk(a, _F64, self.ndof, "a")
         _chk(b, _F64, self.ndof, "b")

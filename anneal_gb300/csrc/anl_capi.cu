@@ -429,6 +429,18 @@ int anl_profile_apply(anl_ctx* ctx, const void* u, void* y, int reps, double* ms
     return solver_profile_apply(ctx, u, y, reps, ms_h, S(stream));
 }
 
+int anl_mg_info(anl_ctx* ctx, int* nlev_h, int* dims_h, double* lmax_h) {
+    NEED(ctx && nlev_h && dims_h && lmax_h, "anl_mg_info: null argument");
+    *nlev_h = (int)ctx->lev.size();
+    for (size_t l = 0; l < ctx->lev.size() && l < 16; ++l) {
+        dims_h[3 * l] = ctx->lev[l].d.nx;
+        dims_h[3 * l + 1] = ctx->lev[l].d.ny;
+        dims_h[3 * l + 2] = ctx->lev[l].d.nz;
+        lmax_h[l] = ctx->lev[l].lmax;
+    }
+    return ANL_OK;
+}
+
 int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const float* xphys, const float* phi,
                      const uint8_t* frozen, double* out_h, anl_stream_t stream) {
     NEED(ctx && xold && xnew && xphys && phi && frozen && out_h, "anl_design_stats: null argument");

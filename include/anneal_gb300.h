@@ -135,6 +135,11 @@ int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const f
 
 /* ---------------------------------------------------------------- measurement */
 
+/* Multigrid hierarchy of the context (no counterpart in the reference): *nlev_h levels,
+   dims_h[3*l..3*l+2] the element dims of level l, lmax_h[l] the estimated largest
+   eigenvalue of D^-1 K used by its Chebyshev smoother (arrays of 16 entries). */
+int anl_mg_info(anl_ctx* ctx, int* nlev_h, int* dims_h, double* lmax_h);
+
 /* Number of kernels this library has launched in the process so far (no counterpart in
    the reference; lets a benchmark count the GPU launches inside its timed region). */
 int64_t anl_launch_count(void);
