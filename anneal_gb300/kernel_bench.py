@@ -1,0 +1,48 @@
+"""Microbenchmark of the matrix-free K u kernel on a clamped box.
+
+    python -m anneal_gb300.kernel_bench [--shape NX NY NZ] [--reps R] [--fp64]
+
+Prints one JSON line: milliseconds per launch (CUDA events, after warm-up), the
+algorithmic bytes (24 per node + 4 per element: read u, write y, read the element
+scale) and the achieved GB/s and FP32 TFLOP/s (1152 flop per element).
+"""
+import argparse
+import json
+
+import numpy as np
+import torch
+
+from .context import Context, to_dev
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--shape", type=int, nargs=3, default=[320, 160, 160])
+    ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--fp64", action="store_true")
+    a = ap.parse_args()
+    nx, ny, nz = a.shape
+    ctx = Context((nx, ny, nz), 1.0, 0.3, fp64=a.fp64)
+    ne, nn = ctx.ne, ctx.nn
+    fixed = np.zeros(3 * nn, np.uint8)
+    clamp = np.arange(0, nn, nx + 1)          # the nodes of the x = 0 face
+    for c in range(3):
+        fixed[3 * clamp + c] = 1
+    ctx.set_domain(torch.ones(ne, dtype=torch.uint8, device="cuda"), to_dev(fixed, torch.uint8))
+    g = torch.Generator(device="cuda").manual_seed(0)
+    E = torch.rand(ne, device="cuda", generator=g, dtype=torch.float32) + 1e-3
+    dt = torch.float64 if a.fp64 else torch.float32
+    mask = ctx.free_mask().to(dt)
+    u = torch.randn(ctx.ndof, device="cuda", generator=g, dtype=dt) * mask
+    y = torch.empty_like(u)
+    ctx.apply_K(E, u, y)
+    ms = ctx.profile_apply(u, y, a.reps)
+    alg = 24 * nn + 4 * ne
+    print(json.dumps({"kernel": "K u (APPLY)", "shape": [nx, ny, nz], "precision": "fp64" if a.fp64 else "fp32",
+                      "ms_per_launch": ms, "algorithmic_bytes": alg, "GBps": alg / (ms * 1e-3) / 1e9,
+                      "tflops": 1152.0 * ne / (ms * 1e-3) / 1e12}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
