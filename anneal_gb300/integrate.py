@@ -1,0 +1,42 @@
+"""Route an installed anneal (0.3.0) through the GPU path.
+
+    import anneal_gb300.integrate as gi
+    gi.install()          # before `anneal run` / `anneal validate` does its work
+
+``install`` swaps the reference's solve and optimise entry points for the GPU ones in the
+already imported (or importable) ``anneal`` package: ``anneal.fem.FEM`` / ``SolverError``,
+``anneal.optimize.simp`` / ``Filter``, the names ``run.py`` bound at import
+(``anneal.run.FEM``, ``anneal.run.simp``) and the validation gate's checks. Spec parsing,
+exports, reports and the database stay the reference's.
+"""
+import importlib
+
+
+def install(anneal_pkg="anneal"):
+    from . import fem as gfem
+    from . import optimize as gopt
+    from . import validate as gval
+    fem = importlib.import_module(f"{anneal_pkg}.fem")
+    opt = importlib.import_module(f"{anneal_pkg}.optimize")
+    fem.FEM = gfem.FEM
+    fem.SolverError = gfem.SolverError
+    fem.hex8_matrices = gfem.hex8_matrices
+    opt.FEM = gfem.FEM
+    opt.simp = gopt.simp
+    opt.Filter = gopt.Filter
+    opt.benchmark_cantilever = gopt.benchmark_cantilever
+    try:
+        run = importlib.import_module(f"{anneal_pkg}.run")
+        run.FEM = gfem.FEM
+        run.simp = gopt.simp
+    except ImportError:   # run.py needs trimesh / skimage / matplotlib
+        pass
+    try:
+        val = importlib.import_module(f"{anneal_pkg}.validate")
+        val.CHECKS = list(gval.CHECKS)
+        val.FEM = gfem.FEM
+    except ImportError:
+        pass
+    # keep the EMIN constant shared: the GPU simp reads anneal_gb300.optimize.EMIN
+    gopt.EMIN = getattr(opt, "EMIN", gopt.EMIN)
+    return True
