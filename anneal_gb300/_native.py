@@ -29,7 +29,7 @@ EXPORTS = [
     "anl_free_mask", "anl_apply_K", "anl_solve", "anl_dot", "anl_element_energy",
     "anl_sensitivity", "anl_stiffness_scale", "anl_filter_init", "anl_filter_fwd",
     "anl_filter_bwd", "anl_physical", "anl_oc_update", "anl_design_stats", "anl_profile_apply",
-    "anl_launch_count", "anl_mg_info",
+    "anl_launch_count", "anl_mg_info", "anl_dot_static",
 ]
 
 
@@ -70,6 +70,7 @@ _SIGS = {
     "anl_profile_apply": (I, [P, P, P, I, ctypes.POINTER(D), P]),
     "anl_launch_count": (I64, []),
     "anl_mg_info": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)]),
+    "anl_dot_static": (I, [P, P, I64, P, P]),
 }
 
 

@@ -133,6 +133,21 @@ int anl_oc_update(anl_ctx* ctx, const float* x, const float* dcx, const float* d
 int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const float* xphys,
                      const float* phi, const uint8_t* frozen, double* out_h, anl_stream_t stream);
 
+/* ---------------------------------------------------------------- allocation-free variant */
+
+/* No counterpart in the reference. The compliance dot product of anl_dot (sum of a[i]*b[i],
+   FP64, deterministic) for callers that cannot allocate device memory: code inside a CUDA
+   host callback or memory-pool hook, embedders whose framework owns the whole device pool,
+   and loops that must not allocate (or synchronise) mid-step. It needs no context: a, b
+   (n doubles) and out (one double) are caller-owned device buffers; the result is written
+   to *out on `stream`. The reduction scratch is a fixed 33 KB array in the library's device
+   memory, held by every GPU that loads the library until the process exits; n may be at
+   most 268,435,456 (ANL_ERR_BADARG beyond). The first call on a device looks up that array's
+   device address (cudaGetSymbolAddress), so make it before any stream capture. Calls share
+   the array: calls that overlap on the GPU (other streams, other threads) race. Allocates
+   nothing, frees nothing. */
+int anl_dot_static(const double* a, const double* b, int64_t n, double* out, anl_stream_t stream);
+
 /* ---------------------------------------------------------------- measurement */
 
 /* Multigrid hierarchy of the context (no counterpart in the reference): *nlev_h levels,
