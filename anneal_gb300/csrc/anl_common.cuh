@@ -122,13 +122,17 @@ __device__ __forceinline__ void block_sum(double (&val)[NV], double* smem /* NV*
     }
 }
 
-// Finishes a reduction: block `bid` of `nblocks` stores its NV partials; the last block
-// sums them in block order into out[0..NV). Call with every thread of the block after
-// block_sum. Returns true in the block (thread 0) that wrote the result.
-template <int NV>
-__device__ __forceinline__ bool finish_reduction(const double (&val)[NV], int bid, int nblocks,
-                                                 double* partials, unsigned* counter, double* out, int tid) {
+// Finishes a reduction: block `bid` of `nblocks` stores its NV partials; the last block to
+// arrive adds them and writes out[0..NV) (from thread 0). The last block sums in parallel:
+// thread t adds partials t, t+NT, t+2NT, ... in order, then a fixed tree combines the
+// threads, so the result depends only on the partials, never on which block came last.
+// Call with every thread of the block after block_sum (val valid in thread 0); `smem` holds
+// NV*NT/32 doubles. Returns true in the block that wrote the result.
+template <int NV, int NT>
+__device__ __forceinline__ bool finish_reduction(const double (&val)[NV], int bid, int nblocks, double* partials,
+                                                 unsigned* counter, double* out, int tid, double* smem) {
     __shared__ bool last;
+    __syncthreads();  // smem of block_sum is reused below
     if (tid == 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) partials[(int64_t)bid * NV + v] = val[v];
@@ -139,12 +143,17 @@ __device__ __forceinline__ bool finish_reduction(const double (&val)[NV], int bi
     __syncthreads();
     if (!last) return false;
     __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+        for (int b = tid; b < nblocks; b += NT) s += __ldcg(partials + (int64_t)b * NV + v);
+        acc[v] = s;
+    }
+    block_sum<NV, NT>(acc, smem, tid);
     if (tid == 0) {
-        for (int v = 0; v < NV; ++v) {
-            double s = 0;
-            for (int b = 0; b < nblocks; ++b) s += ((volatile double*)partials)[(int64_t)b * NV + v];
-            out[v] = s;
-        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[v] = acc[v];
         *counter = 0u;
     }
     return true;

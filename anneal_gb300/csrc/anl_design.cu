@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
         double v[1] = {vol};
         block_sum<1, FT_N>(v, red, tid);
         const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        finish_reduction<1>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out, tid);
+        finish_reduction<1, FT_N>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out, tid, red);
     }
 }
 
@@ -353,7 +353,7 @@ __global__ void k_oc_scale(int64_t ne, const uint8_t* active, const uint8_t* fro
             v[2] += 1.0;
         }
     block_sum<3, DT>(v, sm, threadIdx.x);
-    finish_reduction<3>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
+    finish_reduction<3, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 // With no projection the volume is linear in xn: vol = sum_j wv_j xn_j + sum_frozen phi,
@@ -370,7 +370,7 @@ __global__ void k_oc_vol_linear(int64_t ne, const uint8_t* active, const uint8_t
         }
     double v[1] = {acc.value()};
     block_sum<1, DT>(v, sm, threadIdx.x);
-    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
+    finish_reduction<1, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,
@@ -383,7 +383,7 @@ __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* f
         if (a && fz) f[0] += phi[e];
     }
     block_sum<1, DT>(f, sm, threadIdx.x);
-    finish_reduction<1>(f, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
+    finish_reduction<1, DT>(f, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 __global__ void k_oc_final(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x, const float* dcx,
@@ -470,53 +470,70 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
 
 __global__ void k_stats(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* xold, const float* xnew,
                         const float* xphys, const float* phi, double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[3 * DT / 32];
-    __shared__ float smax[DT / 32];
-    double v[3] = {0, 0, 0};
-    float mx = 0.f;
+    __shared__ double sm[4 * DT / 32];
+    __shared__ bool last;
+    double v[4] = {0, 0, 0, 0};   // grey count, design count, volume, max change
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
         if (!active[e]) continue;
         const float xp = xphys[e];
         v[2] += (double)phi[e] * (double)xp;
         if (!frozen[e]) {
-            mx = fmaxf(mx, fabsf(xnew[e] - xold[e]));
+            v[3] = fmax(v[3], (double)fabsf(xnew[e] - xold[e]));
             if (xp > 0.1f && xp < 0.9f) v[0] += 1.0;
             v[1] += 1.0;
         }
     }
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
-    block_sum<3, DT>(v, sm, threadIdx.x);
-    if (threadIdx.x == 0) {
-        for (int w = 0; w < DT / 32; ++w) mx = fmaxf(mx, smax[w]);
-    }
-    double vals[4] = {v[0], v[1], v[2], (double)mx};
-    // the max is exact in any order; store it through the same deterministic path
-    __shared__ double res[4];
-    if (threadIdx.x == 0) {
-        partials[(int64_t)blockIdx.x * 4 + 0] = vals[0];
-        partials[(int64_t)blockIdx.x * 4 + 1] = vals[1];
-        partials[(int64_t)blockIdx.x * 4 + 2] = vals[2];
-        partials[(int64_t)blockIdx.x * 4 + 3] = vals[3];
-        __threadfence();
-        const unsigned t = atomicAdd(counter, 1u);
-        if (t == gridDim.x - 1) {
-            __threadfence();
-            double s0 = 0, s1 = 0, s2 = 0, m = 0;
-            for (unsigned b = 0; b < gridDim.x; ++b) {
-                const volatile double* pb = partials + (int64_t)b * 4;
-                s0 += pb[0];
-                s1 += pb[1];
-                s2 += pb[2];
-                m = fmax(m, pb[3]);
-            }
-            res[0] = m;
-            res[1] = s1 > 0 ? s0 / s1 : 0.0;
-            res[2] = s2;
-            res[3] = s1;
-            for (int q = 0; q < 4; ++q) out[q] = res[q];
-            *counter = 0u;
+    // block: sums for 0..2, max for 3 (exact in any order)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = 0; q < 4; ++q) {
+        double x = v[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = q == 3 ? fmax(x, y) : x + y;
         }
+        if (lane == 0) sm[q * (DT / 32) + warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 4; ++q) {
+            double x = q == 3 ? 0.0 : 0.0;
+            for (int w = 0; w < DT / 32; ++w) x = q == 3 ? fmax(x, sm[q * (DT / 32) + w]) : x + sm[q * (DT / 32) + w];
+            partials[(int64_t)blockIdx.x * 4 + q] = x;
+        }
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double a[4] = {0, 0, 0, 0};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += DT)
+        for (int q = 0; q < 4; ++q) {
+            const double x = __ldcg(partials + (int64_t)b * 4 + q);
+            a[q] = q == 3 ? fmax(a[q], x) : a[q] + x;
+        }
+    __syncthreads();
+    for (int q = 0; q < 4; ++q) {
+        double x = a[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(0xffffffffu, x, o);
+            x = q == 3 ? fmax(x, y) : x + y;
+        }
+        if (lane == 0) sm[q * (DT / 32) + warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r[4];
+        for (int q = 0; q < 4; ++q) {
+            double x = 0.0;
+            for (int w = 0; w < DT / 32; ++w) x = q == 3 ? fmax(x, sm[q * (DT / 32) + w]) : x + sm[q * (DT / 32) + w];
+            r[q] = x;
+        }
+        out[0] = r[3];
+        out[1] = r[1] > 0 ? r[0] / r[1] : 0.0;
+        out[2] = r[2];
+        out[3] = r[1];
+        *counter = 0u;
     }
 }
 

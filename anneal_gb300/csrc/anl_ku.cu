@@ -13,6 +13,8 @@
 // Tiling: a CTA of 32x8 threads owns a 32x8 column of nodes and marches up a chunk of
 // z-layers, keeping three node planes (with a one-node halo) and two element planes in
 // shared memory. HBM traffic is u once, y once, E once and the node mask once.
+#include <algorithm>
+
 #include "anl_common.cuh"
 #include "anl_kernels.cuh"
 
@@ -38,10 +40,26 @@ struct DotAcc<double> {
     __device__ double value() const { return s; }
 };
 
+constexpr int KU_NSLOT = 4;                                            // node-plane ring
+constexpr int KU_ESLOT = 3;                                            // element-layer ring
+constexpr int KU_PLANE = KU_HY * KU_HX * 3;                            // values per node plane
+constexpr int KU_EPLANE = KU_EY * KU_EX;                               // values per element layer
+constexpr int KU_NLOAD = (KU_PLANE + KU_NT - 1) / KU_NT;               // loads per thread per plane
+constexpr int KU_ELOAD = (KU_EPLANE + KU_NT - 1) / KU_NT;
+
+// Pipelining: while a CTA computes node layer k it holds layers k-1..k+1 (and element layers
+// k-1, k) in a 4-slot / 3-slot ring, and the loads of layer k+2 (element layer k+1) are in
+// flight into registers; they are stored into the free slot after the compute, and one
+// barrier per layer publishes them. Each thread's load slots (shared-memory index and offset
+// within a plane) are computed once.
+#ifndef KU_MINB
+#define KU_MINB 3  // resident CTAs per SM the register allocation is sized for
+#endif
+
 template <class T, int MODE>
-__global__ void __launch_bounds__(KU_NT, 2) ku_kernel(KuArgs<T> a, KeBlocks<T> kb) {
-    __shared__ T su[3][KU_HY][KU_HX][3];
-    __shared__ float sE[2][KU_EY][KU_EX];
+__global__ void __launch_bounds__(KU_NT, (sizeof(T) == 8 ? 2 : KU_MINB)) ku_kernel(KuArgs<T> a, KeBlocks<T> kb) {
+    __shared__ T su[KU_NSLOT][KU_PLANE];
+    __shared__ float sE[KU_ESLOT][KU_EPLANE];
     __shared__ double sred[KU_NT / 32];
     if (a.done != nullptr && *a.done) return;
 
@@ -49,49 +67,80 @@ __global__ void __launch_bounds__(KU_NT, 2) ku_kernel(KuArgs<T> a, KeBlocks<T> k
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * KU_BX + tx;
     const int i0 = blockIdx.x * KU_BX, j0 = blockIdx.y * KU_BY, k0 = blockIdx.z * a.kz;
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+    const int64_t nplane = 3 * (int64_t)NXn * NYn, eplane = (int64_t)d.nx * d.ny;
 
-    auto load_nodes = [&](int slot, int kk) {
-        const bool kin = kk >= 0 && kk < NZn;
-        for (int f = tid; f < KU_HY * KU_HX * 3; f += KU_NT) {
-            const int row = f / (KU_HX * 3);
-            const int w = f - row * (KU_HX * 3);
+    int noff[KU_NLOAD];   // offset within a node plane (3*node + c), -1 outside the grid
+    int eoff[KU_ELOAD];   // offset within an element layer, -1 outside
+#pragma unroll
+    for (int q = 0; q < KU_NLOAD; ++q) {
+        const int f = tid + q * KU_NT;
+        noff[q] = -1;
+        if (f < KU_PLANE) {
+            const int row = f / (KU_HX * 3), w = f - row * (KU_HX * 3);
             const int c = w / 3, comp = w - 3 * c;
             const int gi = i0 - 1 + c, gj = j0 - 1 + row;
-            T v = T(0);
-            if (kin && gi >= 0 && gi < NXn && gj >= 0 && gj < NYn) v = a.u[3 * d.node(gi, gj, kk) + comp];
-            su[slot][row][c][comp] = v;
+            if (gi >= 0 && gi < NXn && gj >= 0 && gj < NYn) noff[q] = 3 * (gi + NXn * gj) + comp;
         }
-    };
-    auto load_elems = [&](int slot, int ke) {
-        const bool kin = ke >= 0 && ke < d.nz;
-        for (int f = tid; f < KU_EY * KU_EX; f += KU_NT) {
+    }
+#pragma unroll
+    for (int q = 0; q < KU_ELOAD; ++q) {
+        const int f = tid + q * KU_NT;
+        eoff[q] = -1;
+        if (f < KU_EPLANE) {
             const int row = f / KU_EX, c = f - row * KU_EX;
             const int gi = i0 - 1 + c, gj = j0 - 1 + row;
-            float v = 0.f;
-            if (kin && gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny) v = a.E[d.elem(gi, gj, ke)];
-            sE[slot][row][c] = v;
+            if (gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny) eoff[q] = gi + d.nx * gj;
         }
+    }
+    T rn[KU_NLOAD];
+    float re[KU_ELOAD];
+    auto fetch = [&](int kk, int ke) {
+        const bool kin = kk >= 0 && kk < NZn, ein = ke >= 0 && ke < d.nz;
+        const T* up = a.u + (int64_t)kk * nplane;
+        const float* ep = a.E + (int64_t)ke * eplane;
+#pragma unroll
+        for (int q = 0; q < KU_NLOAD; ++q) rn[q] = (kin && noff[q] >= 0) ? up[noff[q]] : T(0);
+#pragma unroll
+        for (int q = 0; q < KU_ELOAD; ++q) re[q] = (ein && eoff[q] >= 0) ? ep[eoff[q]] : 0.f;
+    };
+    auto store_nodes = [&](int slot) {
+#pragma unroll
+        for (int q = 0; q < KU_NLOAD; ++q)
+            if (tid + q * KU_NT < KU_PLANE) su[slot][tid + q * KU_NT] = rn[q];
+    };
+    auto store_elems = [&](int slot) {
+#pragma unroll
+        for (int q = 0; q < KU_ELOAD; ++q)
+            if (tid + q * KU_NT < KU_EPLANE) sE[slot][tid + q * KU_NT] = re[q];
     };
 
-    load_nodes(0, k0 - 1);
-    load_nodes(1, k0);
-    load_elems(0, k0 - 1);
+    // prologue: node planes k0-1, k0, k0+1 -> slots 0, 1, 2; element layers k0-1, k0 -> 0, 1
+    fetch(k0 - 1, k0 - 1);
+    store_nodes(0);
+    store_elems(0);
+    fetch(k0, k0);
+    store_nodes(1);
+    store_elems(1);
+    fetch(k0 + 1, -1);
+    store_nodes(2);
+    __syncthreads();
+
     DotAcc<T> dot;
     const int i = i0 + tx, j = j0 + ty;
     const int kend = min(k0 + a.kz, NZn);
     for (int k = k0; k < kend; ++k) {
         const int r = k - k0;
-        const int s_lo = r % 3, s_mid = (r + 1) % 3, s_hi = (r + 2) % 3;
-        const int e_lo = r & 1, e_hi = (r + 1) & 1;
-        load_nodes(s_hi, k + 1);
-        load_elems(e_hi, k);
-        __syncthreads();
+        const int s_lo = r & 3, s_mid = (r + 1) & 3, s_hi = (r + 2) & 3, s_next = (r + 3) & 3;
+        const int e_lo = r % 3, e_hi = (r + 1) % 3, e_next = (r + 2) % 3;
+        const bool more = k + 1 < kend;
+        if (more) fetch(k + 2, k + 1);   // in flight during the compute below
         if (i < NXn && j < NYn) {
-            const T* base[3] = {&su[s_lo][0][0][0], &su[s_mid][0][0][0], &su[s_hi][0][0][0]};
+            const T* base[3] = {su[s_lo], su[s_mid], su[s_hi]};
+            const float* Elo = sE[e_lo];
+            const float* Ehi = sE[e_hi];
             T un[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) un[c] = su[s_mid][ty + 1][tx + 1][c];
-            // differences to the 26 neighbours, dl[mz+1][my+1][mx+1][c]
+            for (int c = 0; c < 3; ++c) un[c] = base[1][((ty + 1) * KU_HX + tx + 1) * 3 + c];
             T dl[3][3][3][3];
 #pragma unroll
             for (int mz = 0; mz < 3; ++mz)
@@ -108,7 +157,7 @@ __global__ void __launch_bounds__(KU_NT, 2) ku_kernel(KuArgs<T> a, KeBlocks<T> k
 #pragma unroll
             for (int oct = 0; oct < 8; ++oct) {
                 const int sx = (oct & 1) ? 1 : -1, sy = (oct & 2) ? 1 : -1, sz = (oct & 4) ? 1 : -1;
-                const float Eo = sE[sz > 0 ? e_hi : e_lo][ty + (sy > 0 ? 1 : 0)][tx + (sx > 0 ? 1 : 0)];
+                const float Eo = (sz > 0 ? Ehi : Elo)[(ty + (sy > 0 ? 1 : 0)) * KU_EX + tx + (sx > 0 ? 1 : 0)];
                 esum += Eo;
                 T w[3] = {T(0), T(0), T(0)};
 #pragma unroll
@@ -146,7 +195,7 @@ __global__ void __launch_bounds__(KU_NT, 2) ku_kernel(KuArgs<T> a, KeBlocks<T> k
                     T dn = T(0), xn = T(0);
                     if ((nm >> c) & 1) {
                         const T rc = a.b[3 * n + c] - y[c];
-                        dn = a.c1 * a.dv[3 * n + c] + a.c2 * rc * inv;
+                        dn = (a.c1 != T(0) ? a.c1 * a.dv[3 * n + c] : T(0)) + a.c2 * rc * inv;
                         xn = un[c] + dn;
                     }
                     a.dv[3 * n + c] = dn;
@@ -154,39 +203,48 @@ __global__ void __launch_bounds__(KU_NT, 2) ku_kernel(KuArgs<T> a, KeBlocks<T> k
                 }
             }
         }
+        if (more) {
+            store_nodes(s_next);
+            store_elems(e_next);
+        }
         __syncthreads();
     }
     if (MODE == KU_APPLY_DOT) {
         double v[1] = {dot.value()};
-        // block_sum uses a flat thread index; reshape the 2D block
-        const int lane = tid & 31, warp = tid >> 5;
-        double s = v[0];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) sred[warp] = s;
-        __syncthreads();
-        if (tid == 0) {
-            double t = 0;
-            for (int w = 0; w < KU_NT / 32; ++w) t += sred[w];
-            v[0] = t;
-        }
+        block_sum<1, KU_NT>(v, sred, tid);
         const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        const int nb = gridDim.x * gridDim.y * gridDim.z;
-        __shared__ bool last;
-        if (tid == 0) {
-            a.partials[bid] = v[0];
-            __threadfence();
-            last = atomicAdd(a.counter, 1u) == (unsigned)nb - 1;
-        }
-        __syncthreads();
-        if (last && tid == 0) {
-            __threadfence();
-            double t = 0;
-            for (int b = 0; b < nb; ++b) t += ((volatile double*)a.partials)[b];
-            *a.red_out = t;
-            *a.counter = 0u;
+        finish_reduction<1, KU_NT>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out, tid,
+                                   sred);
+    }
+}
+
+// z-chunking: the CTA count is a near multiple of the resident CTAs (occupancy x SMs), so
+// the last wave is full; chunks stay at least 4 layers deep (2 halo layers per chunk).
+template <class T, int MODE>
+static int ku_chunks(int columns, int NZn) {
+    static int resident = 0;
+    if (resident == 0) {
+        int dev = 0, sms = 1, occ = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ku_kernel<T, MODE>, KU_NT, 0);
+        resident = std::max(1, sms * std::max(1, occ));
+    }
+    int best = 1;
+    double best_score = -1.0;
+    for (int c = 1; c <= std::max(1, NZn / 4); ++c) {
+        const int kz = ceil_div(NZn, c);
+        const int64_t blocks = (int64_t)columns * ceil_div(NZn, kz);
+        const double waves = (double)blocks / resident;
+        const double eff = waves / std::ceil(waves);                 // last-wave fill
+        const double halo = (double)kz / (kz + 2);                    // halo-plane overhead
+        const double score = eff * halo * std::min(1.0, waves);        // need at least one wave
+        if (score > best_score + 1e-9) {
+            best_score = score;
+            best = c;
         }
     }
+    return best;
 }
 
 template <class T>
@@ -194,9 +252,17 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeBlocks<T>& kb, cudaStream
     KuArgs<T> a = args;
     const Dims& d = a.d;
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-    int chunks = ceil_div(NZn, 16);
+    const int gx = ceil_div(NXn, KU_BX), gy = ceil_div(NYn, KU_BY);
+    int chunks = 1;
+    switch (mode) {
+        case KU_APPLY: chunks = ku_chunks<T, KU_APPLY>(gx * gy, NZn); break;
+        case KU_APPLY_DOT: chunks = ku_chunks<T, KU_APPLY_DOT>(gx * gy, NZn); break;
+        case KU_RESID: chunks = ku_chunks<T, KU_RESID>(gx * gy, NZn); break;
+        case KU_CHEB: chunks = ku_chunks<T, KU_CHEB>(gx * gy, NZn); break;
+        default: return ANL_ERR_BADARG;
+    }
     a.kz = ceil_div(NZn, chunks);
-    dim3 grid(ceil_div(NXn, KU_BX), ceil_div(NYn, KU_BY), ceil_div(NZn, a.kz));
+    dim3 grid(gx, gy, ceil_div(NZn, a.kz));
     dim3 block(KU_BX, KU_BY);
     if (mode == KU_APPLY_DOT && (int64_t)grid.x * grid.y * grid.z > a.partial_capacity) {
         set_error("K u dot: %d blocks exceed the reduction scratch (%d)", grid.x * grid.y * grid.z,
@@ -213,7 +279,6 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeBlocks<T>& kb, cudaStream
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }
-
 
 // ------------------------------------------------------------------ accurate residual
 //
@@ -346,18 +411,12 @@ __global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, Ke
         }
         __syncthreads();
     }
-    const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) rr += __shfl_down_sync(0xffffffffu, rr, o);
-    if (lane == 0) sred[warp] = rr;
-    __syncthreads();
-    double v[1] = {0.0};
-    if (tid == 0)
-        for (int w = 0; w < KU_NT / 32; ++w) v[0] += sred[w];
+    double v[1] = {rr};
+    block_sum<1, KU_NT>(v, sred, tid);
     const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
     const int nb = gridDim.x * gridDim.y * gridDim.z;
     __shared__ double res[1];
-    if (finish_reduction<1>(v, bid, nb, a.partials, a.counter, res, tid)) {
+    if (finish_reduction<1, KU_NT>(v, bid, nb, a.partials, a.counter, res, tid, sred)) {
         if (tid == 0) *a.rr_out = res[0];
     }
 }
@@ -379,11 +438,10 @@ int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, cudaStre
     return ANL_OK;
 }
 
+// Upper bound of the K u grid (chunks of at least 4 layers): sizes the reduction scratch.
 int ku_grid_blocks(const Dims& d) {
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-    const int chunks = ceil_div(NZn, 16);
-    const int kz = ceil_div(NZn, chunks);
-    return ceil_div(NXn, KU_BX) * ceil_div(NYn, KU_BY) * ceil_div(NZn, kz);
+    return ceil_div(NXn, KU_BX) * ceil_div(NYn, KU_BY) * std::max(1, NZn / 4 + 1);
 }
 
 template int launch_ku<float>(int, const KuArgs<float>&, const KeBlocks<float>&, cudaStream_t);

@@ -116,7 +116,7 @@ __global__ void k_count_free(int64_t nn, const uint8_t* nmask, double* partials,
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x)
         v[0] += (double)__popc(nmask[n] & 7);
     block_sum<1, VT>(v, sm, threadIdx.x);
-    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
+    finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 __global__ void k_level0_E(int64_t ne, const float* escale, const uint8_t* active, float h, float* E) {
@@ -268,7 +268,7 @@ __global__ void k_dot_diag(int64_t nn, const T* v, const float* diag, double* pa
     }
     double val[1] = {s.get()};
     block_sum<1, VT>(val, sm, threadIdx.x);
-    finish_reduction<1>(val, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
+    finish_reduction<1, VT>(val, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 // ------------------------------------------------------------------ coarsest grid (FP64)
@@ -404,7 +404,7 @@ __global__ void k_dot_d(int64_t n, const double* a, const double* b, double* par
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[0] = fma(a[i], b[i], v[0]);
     block_sum<1, VT>(v, sm, threadIdx.x);
-    finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x);
+    finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 // x (FP64) -> hi + lo in T
@@ -432,7 +432,7 @@ __global__ void k_true_resid(int64_t n, const double* b, const T* y1, const T* y
     }
     block_sum<1, VT>(v, sm, threadIdx.x);
     __shared__ double res[1];
-    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x)) {
+    if (finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
         if (threadIdx.x == 0) {
             sc->rr_true = res[0];
             if (set_state) {
@@ -476,7 +476,7 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
     double v[2] = {a.get(), b.get()};
     block_sum<2, VT>(v, sm, threadIdx.x);
     __shared__ double res[2];
-    if (finish_reduction<2>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x)) {
+    if (finish_reduction<2, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
         if (threadIdx.x == 0) {
             const int it = sc->iters;
             sc->rz[it & 1] = res[0];
@@ -528,7 +528,7 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
     double v[1] = {rr.get()};
     block_sum<1, VT>(v, sm, threadIdx.x);
     __shared__ double res[1];
-    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x)) {
+    if (finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
         if (threadIdx.x == 0) {
             sc->alpha = alpha;
             sc->rr = res[0];

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kStaticThreads) k_dot_static(const double* a, 
     block_sum<1, kStaticThreads>(v, sm, threadIdx.x);
     unsigned* counter = reinterpret_cast<unsigned*>(scratch + kStaticBlocks);
     __shared__ double res[1];
-    if (finish_reduction<1>(v, blockIdx.x, gridDim.x, scratch, counter, res, threadIdx.x)) {
+    if (finish_reduction<1, kStaticThreads>(v, blockIdx.x, gridDim.x, scratch, counter, res, threadIdx.x, sm)) {
         if (threadIdx.x == 0) *out = res[0];
     }
 }
