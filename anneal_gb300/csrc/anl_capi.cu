@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -15,6 +16,7 @@ static thread_local char g_err[512] = "";
 static std::atomic<long long> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -124,6 +126,7 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
 int design_stats(anl_ctx* c, const float* xold, const float* xnew, const float* xphys, const float* phi,
                  const uint8_t* frozen, double* out, cudaStream_t s);
 int ku_grid_blocks(const Dims& d);
+void ku_prepare();
 int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* ms, cudaStream_t s);
 
 // ------------------------------------------------------------------ context
@@ -166,6 +169,8 @@ static void free_ctx(anl_ctx* c) {
     f(c->filt.Hs);
     f(c->ftmp);
     f(c->ftmp2);
+    if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->sc_h) cudaFreeHost(c->sc_h);
     if (c->red_h) cudaFreeHost(c->red_h);
     delete c;
@@ -268,6 +273,13 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     ALLOC(c->ftmp, ne * sizeof(float));
     ALLOC(c->ftmp2, ne * sizeof(float));
 #undef ALLOC
+    if (cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("stream creation failed");
+        free_ctx(c);
+        return ANL_ERR_CUDA;
+    }
+    c->use_graph = std::getenv("ANL_NO_GRAPH") == nullptr;
+    ku_prepare();
     if (cudaMallocHost((void**)&c->sc_h, sizeof(PcgScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->red_h, 16 * sizeof(double)) != cudaSuccess) {
         set_error("pinned host allocation failed");

@@ -47,6 +47,7 @@ namespace anl {
 
 void set_error(const char* fmt, ...);
 void count_launch();
+void count_launches(long long n);  // kernels replayed by a CUDA graph
 
 // ------------------------------------------------------------------ grid
 

@@ -84,6 +84,14 @@ struct anl_ctx {
     double* red_h = nullptr;    // pinned host mirror
     int part_cap = 0;
 
+    // the CG iteration chunk as a CUDA graph, captured on an internal stream and replayed on
+    // the caller's stream; invalidated whenever the hierarchy's smoother spectra change
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t cg_exec = nullptr;
+    bool cg_valid = false;
+    int cg_nodes = 0;
+    bool use_graph = true;
+
     anl::FilterState filt;
     float* ftmp = nullptr;   // element-field scratch (ne)
     float* ftmp2 = nullptr;  // element-field scratch (ne)

@@ -247,6 +247,18 @@ static int ku_chunks(int columns, int NZn) {
     return best;
 }
 
+// Evaluates the occupancy of every K u variant once (outside any stream capture).
+void ku_prepare() {
+    ku_chunks<float, KU_APPLY>(1, 8);
+    ku_chunks<float, KU_APPLY_DOT>(1, 8);
+    ku_chunks<float, KU_RESID>(1, 8);
+    ku_chunks<float, KU_CHEB>(1, 8);
+    ku_chunks<double, KU_APPLY>(1, 8);
+    ku_chunks<double, KU_APPLY_DOT>(1, 8);
+    ku_chunks<double, KU_RESID>(1, 8);
+    ku_chunks<double, KU_CHEB>(1, 8);
+}
+
 template <class T>
 int launch_ku(int mode, const KuArgs<T>& args, const KeBlocks<T>& kb, cudaStream_t s) {
     KuArgs<T> a = args;

@@ -649,6 +649,7 @@ static int update_hierarchy(anl_ctx* c, bool rebuild, cudaStream_t s) {
     }
     const bool first = !c->coarse_ready;
     if (rebuild || first) {
+        c->cg_valid = false;  // the Chebyshev coefficients in the captured graph change
         const size_t nsm = c->dense_coarse ? c->lev.size() - 1 : c->lev.size();
         for (size_t l = 0; l < nsm; ++l) ANL_TRY(estimate_lmax<T>(c, c->lev[l], s));
         if (c->dense_coarse) ANL_TRY(coarse_factor(c, s));
@@ -778,6 +779,66 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s) {
     return ANL_OK;
 }
 
+// `chunk` CG iterations: V-cycle, r.z and z.q, direction update, q = K p with p.q, then the
+// x / r update with ||r||^2. Every kernel returns early once the device "done" flag is set.
+template <class T>
+static int enqueue_chunk(anl_ctx* c, int chunk, cudaStream_t s) {
+    Level& L0 = c->lev[0];
+    const int64_t n = 3 * L0.d.nn();
+    int* restart = c->flag_d + 1;
+    const int* done = &c->sc->done;
+    for (int k = 0; k < chunk; ++k) {
+        ANL_TRY(vcycle<T>(c, 0, done, s));
+        const T* z = (const T*)L0.x;
+        k_dots_rz_zq<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)L0.b, z, (const T*)c->q, c->sc, restart, c->partials,
+                                                 c->counter);
+        ANL_LAUNCH_CHECK();
+        k_pupdate<T><<<vgrid(n), VT, 0, s>>>(n, z, (T*)c->p, c->sc, restart);
+        ANL_LAUNCH_CHECK();
+        ANL_TRY(apply_level<T>(c, L0, (const T*)c->p, (T*)c->q, s, &c->sc->pq, done));
+        k_axpy<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)c->p, (const T*)c->q, c->xbuf, (T*)L0.b, c->sc, restart,
+                                          c->partials, c->counter);
+        ANL_LAUNCH_CHECK();
+    }
+    return ANL_OK;
+}
+
+// Captures enqueue_chunk into a graph on the context's own stream (the caller's stream may
+// be the legacy default stream, which cannot be captured). The V-cycle's buffer swaps come
+// back to their starting state after an even number of cycles, so the captured pointers
+// stay valid for every replay.
+template <class T>
+static int capture_chunk(anl_ctx* c, int chunk) {
+    if (c->cg_exec) {
+        cudaGraphExecDestroy(c->cg_exec);
+        c->cg_exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    ANL_CUDA(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const int st = enqueue_chunk<T>(c, chunk, c->cap_stream);
+    const cudaError_t e = cudaStreamEndCapture(c->cap_stream, &g);
+    if (st != ANL_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) {
+        set_error("CG graph capture failed: %s", cudaGetErrorString(e));
+        return ANL_ERR_CUDA;
+    }
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    const cudaError_t ei = cudaGraphInstantiate(&c->cg_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        set_error("CG graph instantiation failed: %s", cudaGetErrorString(ei));
+        c->cg_exec = nullptr;
+        return ANL_ERR_CUDA;
+    }
+    c->cg_nodes = (int)nodes;
+    c->cg_valid = true;
+    return ANL_OK;
+}
+
 template <class T>
 static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxiter, int* iters, double* relres,
                    cudaStream_t s) {
@@ -809,22 +870,16 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
     double rr_replace = c->sc_h->rr;  // ||r||^2 at the last replacement
     double stag_ref = -1.0;            // true ||r||^2 when the recurrence first claimed convergence
     int status = ANL_OK;
-    const int chunk = 4;
+    const int chunk = 4;  // even: the V-cycle buffer swaps return to their start (graph replay)
     // (done == 1 here: the initial guess already satisfies the tolerance)
     while (c->sc_h->done != 1) {
         if (c->sc_h->done == 0) {
-            for (int k = 0; k < chunk; ++k) {
-                ANL_TRY(vcycle<T>(c, 0, done, s));
-                const T* z = (const T*)L0.x;
-                k_dots_rz_zq<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)L0.b, z, (const T*)c->q, c->sc, restart,
-                                                         c->partials, c->counter);
-                ANL_LAUNCH_CHECK();
-                k_pupdate<T><<<vgrid(n), VT, 0, s>>>(n, z, (T*)c->p, c->sc, restart);
-                ANL_LAUNCH_CHECK();
-                ANL_TRY(apply_level<T>(c, L0, (const T*)c->p, (T*)c->q, s, &c->sc->pq, done));
-                k_axpy<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)c->p, (const T*)c->q, c->xbuf, (T*)L0.b, c->sc, restart,
-                                                  c->partials, c->counter);
-                ANL_LAUNCH_CHECK();
+            if (c->use_graph) {
+                if (!c->cg_valid) ANL_TRY(capture_chunk<T>(c, chunk));
+                ANL_CUDA(cudaGraphLaunch(c->cg_exec, s));
+                count_launches(c->cg_nodes);
+            } else {
+                ANL_TRY(enqueue_chunk<T>(c, chunk, s));
             }
             ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
             ANL_CUDA(cudaStreamSynchronize(s));
