@@ -104,6 +104,55 @@ double ke_blocks(const double* ke, KeBlocks<double>* out) {
     return dev;
 }
 
+double ke_modal(const double* ke, KeModal<double>* out) {
+    // KA = T^T Ke T with T[3a+c][3m+c] = s_m(p_a), modes 1, sx, sy, sz, sx sy, sy sz, sz sx, sx sy sz
+    double S[8][8];
+    for (int a = 0; a < 8; ++a) {
+        const double sx = 2 * LOCAL[a][0] - 1, sy = 2 * LOCAL[a][1] - 1, sz = 2 * LOCAL[a][2] - 1;
+        const double m[8] = {1, sx, sy, sz, sx * sy, sy * sz, sz * sx, sx * sy * sz};
+        for (int q = 0; q < 8; ++q) S[a][q] = m[q];
+    }
+    auto ka = [&](int m, int c, int n, int e) {  // KA[(m,c),(n,e)] / 64
+        double s = 0;
+        for (int a = 0; a < 8; ++a)
+            for (int b = 0; b < 8; ++b) s += S[a][m] * ke[(3 * a + c) * 24 + 3 * b + e] * S[b][n];
+        return s / 64.0;
+    };
+    const double A = ka(1, 0, 1, 0), B = ka(1, 0, 2, 1), C = ka(1, 1, 1, 1), D = ka(4, 0, 4, 0),
+                 F = ka(4, 0, 5, 2), G = ka(4, 2, 4, 2), H = ka(4, 2, 5, 0), J = ka(7, 0, 7, 0);
+    *out = KeModal<double>{A - B, B, C, D, F, G - H, H, J};
+    // rebuild Ke column by column through modal_element and compare
+    double kmax = 0.0, dev = 0.0;
+    for (int t = 0; t < 576; ++t) kmax = std::max(kmax, std::fabs(ke[t]));
+    for (int col = 0; col < 24; ++col) {
+        double u[2][2][2][3] = {};
+        const int bn = col / 3;
+        u[LOCAL[bn][0]][LOCAL[bn][1]][LOCAL[bn][2]][col % 3] = 1.0;
+        auto v3 = [&](int px, int py, int pz) {
+            V3<double> v;
+            v.xy.x = u[px][py][pz][0];
+            v.xy.y = u[px][py][pz][1];
+            v.z = u[px][py][pz][2];
+            return v;
+        };
+        V3<double> dxb[2], dxt[2], dyb[2], dyt[2], dz[2][2], f[2][2][2];
+        for (int q = 0; q < 2; ++q) {
+            dxb[q] = v3(1, q, 0) - v3(0, q, 0);
+            dxt[q] = v3(1, q, 1) - v3(0, q, 1);
+            dyb[q] = v3(q, 1, 0) - v3(q, 0, 0);
+            dyt[q] = v3(q, 1, 1) - v3(q, 0, 1);
+            for (int r = 0; r < 2; ++r) dz[q][r] = v3(q, r, 1) - v3(q, r, 0);
+        }
+        modal_element<double>(*out, 1.0, dxb, dxt, dyb, dyt, dz, f);
+        for (int a = 0; a < 8; ++a) {
+            const V3<double>& fa = f[LOCAL[a][0]][LOCAL[a][1]][LOCAL[a][2]];
+            const double fc[3] = {fa.xy.x, fa.xy.y, fa.z};
+            for (int c = 0; c < 3; ++c) dev = std::max(dev, std::fabs(fc[c] - ke[(3 * a + c) * 24 + col]));
+        }
+    }
+    return dev / kmax;
+}
+
 // ------------------------------------------------------------------ declarations from other units
 
 int solver_setup_domain(anl_ctx* c, const uint8_t* active, const uint8_t* fixed, cudaStream_t s);
@@ -199,6 +248,14 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     }
     for (int a = 0; a < 8; ++a)
         for (int t = 0; t < 9; ++t) c->kbf.blk[a][t] = (float)c->kbd.blk[a][t];
+    const double mdev = ke_modal(c->ke, &c->kmd);
+    if (!(mdev < 1e-12)) {
+        set_error("element matrix lacks the isotropic mode structure (deviation %g)", mdev);
+        free_ctx(c);
+        return ANL_ERR_BADARG;
+    }
+    c->kmf = KeModal<float>{(float)c->kmd.ab, (float)c->kmd.b, (float)c->kmd.c,  (float)c->kmd.d,
+                            (float)c->kmd.f,  (float)c->kmd.gh, (float)c->kmd.h, (float)c->kmd.j};
     c->kdiag = c->ke[0];
 
 #define ALLOC(ptr, bytes)                                                  \

@@ -85,6 +85,142 @@ void hex8_ke(double nu, double h, double* ke);
 // the largest deviation found.
 double ke_blocks(const double* ke, KeBlocks<double>* out);
 
+// The same Ke in the basis of the 8 trilinear modes of a brick. A displacement component
+// on the 8 corners p in {0,1}^3 is a combination of 1, sx, sy, sz, sx sy, sy sz, sz sx,
+// sx sy sz (s = 2p - 1); its mode amplitudes beta_m = sum_p s_m(p) u_p are a Walsh-Hadamard
+// transform. Ke u = T (KA / 64) T^T u with KA = T^T Ke T, and for an isotropic material KA
+// is sparse: 45 non-zeros in 24 x 24, set by 8 numbers (the rigid translations, mode 1, carry
+// none). So one element costs about 200 flops instead of the 1152 of the dense 24 x 24
+// product, and the transform can be taken from edge differences u(p + e_d) - u(p), which
+// keeps FP32 products proportional to the local strain, not to |u|.
+// Constants (of KA / 64; modes x y z xy yz zx xyz = 1..7, components x y z):
+//   g1x = A b1x + B (b2y + b3z)   and cyclic      -> ab = A - B, b = B (trace form)
+//   g1y = g2x = C (b1y + b2x)     and cyclic      -> c
+//   g4x = D b4x + F b5z, g5z = F b4x + D b5z, ... -> d, f
+//   g4z = G b4z + H (b5x + b6y)   and cyclic      -> gh = G - H, h = H
+//   g7c = J b7c                                   -> j
+template <class T>
+struct KeModal {
+    T ab, b, c, d, f, gh, h, j;
+};
+
+// Host: the modal constants of ke (unit E); returns the largest deviation between ke and
+// the matrix that modal_element applies, relative to max |ke| (a full 24 x 24 check).
+double ke_modal(const double* ke, KeModal<double>* out);
+
+// A nodal 3-vector: x and y as a pair, z alone. In FP32 the pair is a float2 driven by the
+// packed f32x2 instructions of sm_100+ (one instruction for both lanes), which takes a third
+// of the instructions out of the element transforms; in FP64 it is two doubles.
+struct dpair {
+    double x, y;
+};
+template <class T>
+struct PairOf;
+template <>
+struct PairOf<float> {
+    using type = float2;
+};
+template <>
+struct PairOf<double> {
+    using type = dpair;
+};
+template <class T>
+struct V3 {
+    typename PairOf<T>::type xy;
+    T z;
+};
+
+__host__ __device__ __forceinline__ dpair padd(dpair a, dpair b) { return {a.x + b.x, a.y + b.y}; }
+__host__ __device__ __forceinline__ dpair psub(dpair a, dpair b) { return {a.x - b.x, a.y - b.y}; }
+__host__ __device__ __forceinline__ dpair pscale(double s, dpair a) { return {s * a.x, s * a.y}; }
+#ifdef __CUDACC__
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) {  // a - b, one rounding
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 pscale(float s, float2 a) { return __fmul2_rn(make_float2(s, s), a); }
+#endif
+
+#pragma nv_exec_check_disable
+template <class T>
+__host__ __device__ __forceinline__ V3<T> operator+(const V3<T>& a, const V3<T>& b) {
+    return V3<T>{padd(a.xy, b.xy), a.z + b.z};
+}
+#pragma nv_exec_check_disable
+template <class T>
+__host__ __device__ __forceinline__ V3<T> operator-(const V3<T>& a, const V3<T>& b) {
+    return V3<T>{psub(a.xy, b.xy), a.z - b.z};
+}
+#pragma nv_exec_check_disable
+template <class T>
+__host__ __device__ __forceinline__ V3<T> operator*(T s, const V3<T>& a) {
+    return V3<T>{pscale(s, a.xy), s * a.z};
+}
+template <class T>
+__host__ __device__ __forceinline__ V3<T> v3zero() {
+    V3<T> v;
+    v.xy.x = T(0);
+    v.xy.y = T(0);
+    v.z = T(0);
+    return v;
+}
+
+// E Ke u_e of one brick from its edge differences (p = corner in {0,1}^3):
+//   dxb[py] = u(1,py,0) - u(0,py,0),  dxt[py] = u(1,py,1) - u(0,py,1)
+//   dyb[px] = u(px,1,0) - u(px,0,0),  dyt[px] = u(px,1,1) - u(px,0,1)
+//   dz[px][py] = u(px,py,1) - u(px,py,0)
+// and writes the corner forces f[px][py][pz].
+#pragma nv_exec_check_disable
+template <class T>
+__host__ __device__ __forceinline__ void modal_element(const KeModal<T>& k, T E, const V3<T> (&dxb)[2],
+                                                       const V3<T> (&dxt)[2], const V3<T> (&dyb)[2],
+                                                       const V3<T> (&dyt)[2], const V3<T> (&dz)[2][2],
+                                                       V3<T> (&f)[2][2][2]) {
+    // mode amplitudes (Walsh-Hadamard transform through the edges)
+    const V3<T> s0 = dxb[0] + dxb[1], s1 = dxt[0] + dxt[1];
+    const V3<T> b1 = s0 + s1, b6 = s1 - s0;
+    const V3<T> p0 = dxb[1] - dxb[0], p1 = dxt[1] - dxt[0];
+    const V3<T> b4 = p0 + p1, b7 = p1 - p0;
+    const V3<T> t0 = dyb[0] + dyb[1], t1 = dyt[0] + dyt[1];
+    const V3<T> b2 = t0 + t1, b5 = t1 - t0;
+    const V3<T> b3 = (dz[0][0] + dz[1][0]) + (dz[0][1] + dz[1][1]);
+    // the sparse modal stiffness, scaled by E
+    const T ab = E * k.ab, bb = E * k.b, cc = E * k.c, dd = E * k.d, ff = E * k.f, gh = E * k.gh, hh = E * k.h,
+            jj = E * k.j;
+    V3<T> g1, g2, g3, g4, g5, g6;
+    const T tr = b1.xy.x + b2.xy.y + b3.z;
+    g1.xy.x = ab * b1.xy.x + bb * tr;
+    g2.xy.y = ab * b2.xy.y + bb * tr;
+    g3.z = ab * b3.z + bb * tr;
+    g1.xy.y = g2.xy.x = cc * (b1.xy.y + b2.xy.x);
+    g1.z = g3.xy.x = cc * (b1.z + b3.xy.x);
+    g2.z = g3.xy.y = cc * (b2.z + b3.xy.y);
+    g4.xy.x = dd * b4.xy.x + ff * b5.z;
+    g5.z = ff * b4.xy.x + dd * b5.z;
+    g4.xy.y = dd * b4.xy.y + ff * b6.z;
+    g6.z = ff * b4.xy.y + dd * b6.z;
+    g5.xy.y = dd * b5.xy.y + ff * b6.xy.x;
+    g6.xy.x = ff * b5.xy.y + dd * b6.xy.x;
+    const T s3 = b4.z + b5.xy.x + b6.xy.y;
+    g4.z = gh * b4.z + hh * s3;
+    g5.xy.x = gh * b5.xy.x + hh * s3;
+    g6.xy.y = gh * b6.xy.y + hh * s3;
+    const V3<T> g7 = jj * b7;
+    // back to the corners: f(p) = sum_m s_m(p) g_m = A(py,pz) + sx B(py,pz)
+    const V3<T> am = g2 - g5, ap = g2 + g5;
+    const V3<T> n00 = am + g3, a10 = am - g3, a01 = g3 - ap, a11 = ap + g3;  // A(0,0) = -n00
+    const V3<T> cm = g1 - g6, cp = g1 + g6, dm = g4 - g7, dp = g4 + g7;
+    const V3<T> q00 = cm - dm, q10 = cm + dm, q01 = cp - dp, q11 = cp + dp;
+    f[0][0][0] = v3zero<T>() - (n00 + q00);
+    f[1][0][0] = q00 - n00;
+    f[0][1][0] = a10 - q10;
+    f[1][1][0] = a10 + q10;
+    f[0][0][1] = a01 - q01;
+    f[1][0][1] = a01 + q01;
+    f[0][1][1] = a11 - q11;
+    f[1][1][1] = a11 + q11;
+}
+
 // ------------------------------------------------------------------ reductions
 
 // Deterministic two-stage reductions: every block writes its partial sums to a scratch

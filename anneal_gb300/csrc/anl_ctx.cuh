@@ -47,6 +47,8 @@ struct anl_ctx {
     double* ke_d = nullptr;         // Ke(1) on the device (coarse assembly)
     anl::KeBlocks<double> kbd{};
     anl::KeBlocks<float> kbf{};
+    anl::KeModal<double> kmd{};
+    anl::KeModal<float> kmf{};
     double kdiag = 0.0;
 
     bool domain_set = false;

@@ -30,7 +30,7 @@ struct KuArgs {
 };
 
 template <class T>
-int launch_ku(int mode, const KuArgs<T>& a, const KeBlocks<T>& kb, cudaStream_t s);
+int launch_ku(int mode, const KuArgs<T>& a, const KeModal<T>& km, cudaStream_t s);
 
 // r = b - K32 x with x = xhi + xlo, evaluated in float-pair arithmetic; ||r||^2 -> *rr_out
 struct ResidHpArgs {

@@ -1,18 +1,21 @@
 // anl_ku.cu -- matrix-free hex8 operator K u and the kernels fused with it.
 //
 // Replaces the assembled CSR matrix of FEM.assemble (fem.py:198-201) and its SpMV inside
-// scipy's CG (fem.py:224). K = sum_e E_e Ke acts node by node (gather form, no atomics):
+// scipy's CG (fem.py:224). K = sum_e E_e Ke is applied element by element in the basis of the
+// trilinear modes (modal_element, anl_common.cuh): about 200 flops per element instead of the
+// 1152 of the dense 24 x 24 product, taken from edge differences so that FP32 products scale
+// with the local strain, not with |u|.
 //
-//   (K u)_n = sum_{octants o} E_o * S_o * sum_{delta != 0} B0(delta) * S_o * (u_{n + o.delta} - u_n)
-//
-// o in {-1,+1}^3 picks the element around node n, S_o = diag(o), B0 are the 8 base 3x3
-// blocks of Ke (anl_common.cuh). The difference form uses the zero block-row sums of Ke;
-// it keeps FP32 products proportional to the local strain rather than to |u|, which is
-// what lets the FP32 operator resolve residuals far below |K| |u| eps.
-//
-// Tiling: a CTA of 32x8 threads owns a 32x8 column of nodes and marches up a chunk of
-// z-layers, keeping three node planes (with a one-node halo) and two element planes in
-// shared memory. HBM traffic is u once, y once, E once and the node mask once.
+// Tiling. A CTA is 32 lanes (x) by NW warps (y) and marches up a chunk of z-layers. Lane l of
+// warp w computes the element column (ie, je) = (30 bx - 1 + l, (NW-1) by - 1 + w): it loads
+// its own two nodes (ie, je) and (ie, je + 1) of each node plane and takes the nodes of column
+// ie + 1 from lane l + 1 by a shuffle. Corner forces are summed onto nodes without atomics:
+// across x by a shuffle from lane l - 1, across y through shared memory from warp w - 1, and
+// across z in registers from the previous layer. So lanes 1..30 of warps 1..NW-1 own complete
+// nodes; the outer lanes and warp 0 compute the halo elements of the tile (a 13 % overlap
+// at NW = 16). Edge differences of the lower node plane are carried from the previous layer,
+// and warps whose 32 elements are all void skip the element arithmetic.
+// HBM traffic is u once, y once, E once and the node mask once (halo re-reads hit L2).
 #include <algorithm>
 
 #include "anl_common.cuh"
@@ -20,10 +23,24 @@
 
 namespace anl {
 
+// the 32x8 tile of the float-pair residual kernel below
 constexpr int KU_BX = 32, KU_BY = 8;
 constexpr int KU_HX = KU_BX + 2, KU_HY = KU_BY + 2;
 constexpr int KU_EX = KU_BX + 1, KU_EY = KU_BY + 1;
 constexpr int KU_NT = KU_BX * KU_BY;
+
+#ifndef KU_NW32
+#define KU_NW32 16  // warps per CTA of the FP32 K u kernel
+#endif
+#ifndef KU_MINB32
+#define KU_MINB32 1  // resident CTAs per SM its registers are sized for
+#endif
+#ifndef KU_DEPTH
+#define KU_DEPTH 3  // layers staged ahead by cp.async
+#endif
+#define KU_RING (KU_DEPTH + 1)
+
+__host__ __device__ constexpr int ceil_div_d(int a, int b) { return (a + b - 1) / b; }
 
 template <class T>
 struct DotAcc;
@@ -40,252 +57,410 @@ struct DotAcc<double> {
     __device__ double value() const { return s; }
 };
 
-constexpr int KU_NSLOT = 4;                                            // node-plane ring
-constexpr int KU_ESLOT = 3;                                            // element-layer ring
-constexpr int KU_PLANE = KU_HY * KU_HX * 3;                            // values per node plane
-constexpr int KU_EPLANE = KU_EY * KU_EX;                               // values per element layer
-constexpr int KU_NLOAD = (KU_PLANE + KU_NT - 1) / KU_NT;               // loads per thread per plane
-constexpr int KU_ELOAD = (KU_EPLANE + KU_NT - 1) / KU_NT;
+// warps per CTA: 16 in FP32 (15 owned node rows), 8 in FP64 (shared memory and registers)
+template <class T>
+struct KmCfg {
+    static constexpr int NW = sizeof(T) == 4 ? KU_NW32 : 8;
+    static constexpr int NT = 32 * NW;
+    static constexpr int OX = 30;      // node columns owned per CTA
+    static constexpr int OY = NW - 1;  // node rows owned per CTA
+    static constexpr int MINB = sizeof(T) == 4 ? KU_MINB32 : 1;
+};
 
-// Pipelining: while a CTA computes node layer k it holds layers k-1..k+1 (and element layers
-// k-1, k) in a 4-slot / 3-slot ring, and the loads of layer k+2 (element layer k+1) are in
-// flight into registers; they are stored into the free slot after the compute, and one
-// barrier per layer publishes them. Each thread's load slots (shared-memory index and offset
-// within a plane) are computed once.
-#ifndef KU_MINB
-#define KU_MINB 3  // resident CTAs per SM the register allocation is sized for
-#endif
+constexpr unsigned FULL = 0xffffffffu;
+
+template <class T>
+__device__ __forceinline__ V3<T> shfl_down3(const V3<T>& v) {
+    V3<T> r;
+    r.xy.x = __shfl_down_sync(FULL, v.xy.x, 1);
+    r.xy.y = __shfl_down_sync(FULL, v.xy.y, 1);
+    r.z = __shfl_down_sync(FULL, v.z, 1);
+    return r;
+}
+template <class T>
+__device__ __forceinline__ V3<T> shfl_up3(const V3<T>& v) {
+    V3<T> r;
+    r.xy.x = __shfl_up_sync(FULL, v.xy.x, 1);
+    r.xy.y = __shfl_up_sync(FULL, v.xy.y, 1);
+    r.z = __shfl_up_sync(FULL, v.z, 1);
+    return r;
+}
+
+// state carried from one element layer to the next (lower node plane of the next layer)
+template <class T>
+struct KuCarry {
+    V3<T> ub[2];   // own nodes (ie, je) and (ie, je + 1)
+    V3<T> dxb[2];  // Dx of rows je, je + 1
+    V3<T> dyb[2];  // Dy of columns ie, ie + 1
+    V3<T> acc;     // forces of the layer below on node (ie, je)
+    float sprev;   // E summed over the 4 elements of the layer below around node (ie, je)
+};
+// epilogue inputs of the next output node, loaded one layer ahead
+template <class T>
+struct KuEpi {
+    uint8_t nm;
+    T b[3], dv[3];
+};
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Shared memory of one CTA: a ring of KU_RING staged (node plane, element layer) pairs filled
+// by cp.async KU_DEPTH layers ahead, and the double-buffered y hand-over between warps (row
+// w + 1 is written by warp w; row 0 stays zero for warp 0).
+template <class T, int MODE>
+struct KuSmem {
+    static constexpr int NW = KmCfg<T>::NW;
+    static constexpr int NV = MODE == KU_CHEB ? 7 : 6;  // values passed to the next warp (+ E sum)
+    T u[KU_RING][NW + 1][32][3];
+    float E[KU_RING][NW][32];
+    T x[2][NW + 1][NV][32];
+};
+static_assert((KU_RING & (KU_RING - 1)) == 0, "the cp.async ring length must be a power of two");
 
 template <class T, int MODE>
-__global__ void __launch_bounds__(KU_NT, (sizeof(T) == 8 ? 2 : KU_MINB)) ku_kernel(KuArgs<T> a, KeBlocks<T> kb) {
-    __shared__ T su[KU_NSLOT][KU_PLANE];
-    __shared__ float sE[KU_ESLOT][KU_EPLANE];
-    __shared__ double sred[KU_NT / 32];
-    if (a.done != nullptr && *a.done) return;
+struct KuTile {
+    static constexpr int NW = KmCfg<T>::NW;
+    using Smem = KuSmem<T, MODE>;
+    static constexpr uint32_t SLOT_U = sizeof(T) * (NW + 1) * 32 * 3;  // bytes per ring slot
+    static constexpr uint32_t SLOT_E = sizeof(float) * NW * 32;
+    const KuArgs<T>& a;
+    const KeModal<T>& km;
+    Smem& sm;
+    int lane, w;
+    int NXn, NYn, NZn;
+    int64_t plane, eplane;
+    uint32_t s_u, s_uN, s_E;  // shared addresses of this thread's ring entries in slot 0
+    // segment geometry
+    bool r0in, rNin, ein, owner;
+    int64_t n0, e0;
+    // staging cursor: next layer ik; sources of node plane ik + 1 and element layer ik
+    int ik;
+    const T* iu;
+    const float* iE;
 
-    const Dims d = a.d;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * KU_BX + tx;
-    const int i0 = blockIdx.x * KU_BX, j0 = blockIdx.y * KU_BY, k0 = blockIdx.z * a.kz;
-    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-    const int64_t nplane = 3 * (int64_t)NXn * NYn, eplane = (int64_t)d.nx * d.ny;
-
-    int noff[KU_NLOAD];   // offset within a node plane (3*node + c), -1 outside the grid
-    int eoff[KU_ELOAD];   // offset within an element layer, -1 outside
-#pragma unroll
-    for (int q = 0; q < KU_NLOAD; ++q) {
-        const int f = tid + q * KU_NT;
-        noff[q] = -1;
-        if (f < KU_PLANE) {
-            const int row = f / (KU_HX * 3), w = f - row * (KU_HX * 3);
-            const int c = w / 3, comp = w - 3 * c;
-            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
-            if (gi >= 0 && gi < NXn && gj >= 0 && gj < NYn) noff[q] = 3 * (gi + NXn * gj) + comp;
-        }
+    __device__ KuTile(const KuArgs<T>& a_, const KeModal<T>& km_, Smem& sm_) : a(a_), km(km_), sm(sm_) {
+        lane = threadIdx.x;
+        w = threadIdx.y;
+        NXn = a.d.nx + 1;
+        NYn = a.d.ny + 1;
+        NZn = a.d.nz + 1;
+        plane = (int64_t)NXn * NYn;
+        eplane = (int64_t)a.d.nx * a.d.ny;
+        s_u = (uint32_t)__cvta_generic_to_shared(&sm.u[0][w][lane][0]);
+        s_uN = (uint32_t)__cvta_generic_to_shared(&sm.u[0][NW][lane][0]);
+        s_E = (uint32_t)__cvta_generic_to_shared(&sm.E[0][w][lane]);
     }
-#pragma unroll
-    for (int q = 0; q < KU_ELOAD; ++q) {
-        const int f = tid + q * KU_NT;
-        eoff[q] = -1;
-        if (f < KU_EPLANE) {
-            const int row = f / KU_EX, c = f - row * KU_EX;
-            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
-            if (gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny) eoff[q] = gi + d.nx * gj;
-        }
+
+    __device__ void set_column(int bx, int by, int k0) {
+        const int ie = bx * KmCfg<T>::OX - 1 + lane, je = by * KmCfg<T>::OY - 1 + w;
+        const bool xin = ie >= 0 && ie < NXn;
+        r0in = xin && je >= 0 && je < NYn;
+        rNin = xin && by * KmCfg<T>::OY - 1 + NW < NYn;  // the extra row of the last warp
+        ein = ie >= 0 && ie < a.d.nx && je >= 0 && je < a.d.ny;
+        owner = lane >= 1 && lane <= KmCfg<T>::OX && w >= 1 && xin && je < NYn;
+        n0 = (int64_t)ie + (int64_t)NXn * je;
+        e0 = (int64_t)ie + (int64_t)a.d.nx * je;
+        ik = k0 - 2;
+        iu = a.u + 3 * (n0 + (int64_t)(ik + 1) * plane);
+        iE = a.E + e0 + (int64_t)ik * eplane;
     }
-    T rn[KU_NLOAD];
-    float re[KU_ELOAD];
-    auto fetch = [&](int kk, int ke) {
-        const bool kin = kk >= 0 && kk < NZn, ein = ke >= 0 && ke < d.nz;
-        const T* up = a.u + (int64_t)kk * nplane;
-        const float* ep = a.E + (int64_t)ke * eplane;
-#pragma unroll
-        for (int q = 0; q < KU_NLOAD; ++q) rn[q] = (kin && noff[q] >= 0) ? up[noff[q]] : T(0);
-#pragma unroll
-        for (int q = 0; q < KU_ELOAD; ++q) re[q] = (ein && eoff[q] >= 0) ? ep[eoff[q]] : 0.f;
-    };
-    auto store_nodes = [&](int slot) {
-#pragma unroll
-        for (int q = 0; q < KU_NLOAD; ++q)
-            if (tid + q * KU_NT < KU_PLANE) su[slot][tid + q * KU_NT] = rn[q];
-    };
-    auto store_elems = [&](int slot) {
-#pragma unroll
-        for (int q = 0; q < KU_ELOAD; ++q)
-            if (tid + q * KU_NT < KU_EPLANE) sE[slot][tid + q * KU_NT] = re[q];
-    };
 
-    // prologue: node planes k0-1, k0, k0+1 -> slots 0, 1, 2; element layers k0-1, k0 -> 0, 1
-    fetch(k0 - 1, k0 - 1);
-    store_nodes(0);
-    store_elems(0);
-    fetch(k0, k0);
-    store_nodes(1);
-    store_elems(1);
-    fetch(k0 + 1, -1);
-    store_nodes(2);
-    __syncthreads();
-
-    DotAcc<T> dot;
-    const int i = i0 + tx, j = j0 + ty;
-    const int kend = min(k0 + a.kz, NZn);
-    for (int k = k0; k < kend; ++k) {
-        const int r = k - k0;
-        const int s_lo = r & 3, s_mid = (r + 1) & 3, s_hi = (r + 2) & 3, s_next = (r + 3) & 3;
-        const int e_lo = r % 3, e_hi = (r + 1) % 3, e_next = (r + 2) % 3;
-        const bool more = k + 1 < kend;
-        if (more) fetch(k + 2, k + 1);   // in flight during the compute below
-        if (i < NXn && j < NYn) {
-            const T* base[3] = {su[s_lo], su[s_mid], su[s_hi]};
-            const float* Elo = sE[e_lo];
-            const float* Ehi = sE[e_hi];
-            T un[3];
+    // stages layer ik (node plane ik + 1, element layer ik) into its ring slot (zeros outside
+    // the grid) when ik < kend, then advances the cursor; one commit group either way
+    __device__ __forceinline__ void issue_next(int kend) {
+        if (ik < kend) {
+            const int pk = ik + 1;
+            const bool kin = pk >= 0 && pk < NZn;
+            const uint32_t so = (uint32_t)(ik & (KU_RING - 1));
+            const bool q0 = kin && r0in;
+            const T* src = q0 ? iu : a.u;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) un[c] = base[1][((ty + 1) * KU_HX + tx + 1) * 3 + c];
-            T dl[3][3][3][3];
-#pragma unroll
-            for (int mz = 0; mz < 3; ++mz)
-#pragma unroll
-                for (int my = 0; my < 3; ++my)
-#pragma unroll
-                    for (int mx = 0; mx < 3; ++mx) {
-                        const T* p = base[mz] + ((ty + my) * KU_HX + (tx + mx)) * 3;
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) dl[mz][my][mx][c] = p[c] - un[c];
-                    }
-            T y[3] = {T(0), T(0), T(0)};
-            float esum = 0.f;
-#pragma unroll
-            for (int oct = 0; oct < 8; ++oct) {
-                const int sx = (oct & 1) ? 1 : -1, sy = (oct & 2) ? 1 : -1, sz = (oct & 4) ? 1 : -1;
-                const float Eo = (sz > 0 ? Ehi : Elo)[(ty + (sy > 0 ? 1 : 0)) * KU_EX + tx + (sx > 0 ? 1 : 0)];
-                esum += Eo;
-                T w[3] = {T(0), T(0), T(0)};
-#pragma unroll
-                for (int dlt = 1; dlt < 8; ++dlt) {
-                    const int dx = dlt & 1, dy = (dlt >> 1) & 1, dz = (dlt >> 2) & 1;
-                    const T* dv = dl[1 + sz * dz][1 + sy * dy][1 + sx * dx];
-                    const T t0 = sx > 0 ? dv[0] : -dv[0];
-                    const T t1 = sy > 0 ? dv[1] : -dv[1];
-                    const T t2 = sz > 0 ? dv[2] : -dv[2];
-                    const T* B = kb.blk[dlt];
-#pragma unroll
-                    for (int rr = 0; rr < 3; ++rr) w[rr] += B[3 * rr] * t0 + B[3 * rr + 1] * t1 + B[3 * rr + 2] * t2;
-                }
-                const T Et = T(Eo);
-                y[0] += sx > 0 ? Et * w[0] : -Et * w[0];
-                y[1] += sy > 0 ? Et * w[1] : -Et * w[1];
-                y[2] += sz > 0 ? Et * w[2] : -Et * w[2];
+            for (int c = 0; c < 3; ++c) {
+                const uint32_t d = s_u + so * SLOT_U + c * (uint32_t)sizeof(T);
+                if (sizeof(T) == 4) cp_async4(d, src + (q0 ? c : 0), q0);
+                else cp_async8(d, src + (q0 ? c : 0), q0);
             }
-            const int64_t n = d.node(i, j, k);
-            const uint8_t nm = a.nmask[n];
+            if (w == NW - 1) {  // node row je + 1 of the last warp
+                const bool qn = kin && rNin;
+                const T* srcn = qn ? iu + 3 * NXn : a.u;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const uint32_t d = s_uN + so * SLOT_U + c * (uint32_t)sizeof(T);
+                    if (sizeof(T) == 4) cp_async4(d, srcn + (qn ? c : 0), qn);
+                    else cp_async8(d, srcn + (qn ? c : 0), qn);
+                }
+            }
+            const bool qe = ein && ik >= 0 && ik < a.d.nz;
+            cp_async4(s_E + so * SLOT_E, qe ? iE : a.E, qe);
+        }
+        cp_async_commit();
+        ++ik;
+        iu += 3 * plane;
+        iE += eplane;
+    }
+
+    __device__ __forceinline__ void node_pair(int slot, V3<T> (&u)[2]) const {
+        const T* p = &sm.u[slot][w][lane][0];
+        constexpr int ROW = 32 * 3;
+        u[0].xy.x = p[0];
+        u[0].xy.y = p[1];
+        u[0].z = p[2];
+        u[1].xy.x = p[ROW];
+        u[1].xy.y = p[ROW + 1];
+        u[1].z = p[ROW + 2];
+    }
+
+    // epilogue loads of output node n (plane kk)
+    __device__ __forceinline__ void epi_load(int64_t n, bool emit, KuEpi<T>& e) const {
+        e.nm = 0;
+        if (emit) {
+            e.nm = __ldg(a.nmask + n);
+            if (MODE == KU_RESID || MODE == KU_CHEB) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) e.b[c] = __ldg(a.b + 3 * n + c);
+            }
+            if (MODE == KU_CHEB) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) e.dv[c] = a.c1 != T(0) ? a.dv[3 * n + c] : T(0);
+            }
+        }
+    }
+
+    // carry of the node plane staged in `slot` (edge differences only, no forces yet)
+    __device__ __forceinline__ void start(int slot, KuCarry<T>& c) const {
+        node_pair(slot, c.ub);
+        const V3<T> nb0 = shfl_down3(c.ub[0]), nb1 = shfl_down3(c.ub[1]);
+        c.dxb[0] = nb0 - c.ub[0];
+        c.dxb[1] = nb1 - c.ub[1];
+        c.dyb[0] = c.ub[1] - c.ub[0];
+        c.dyb[1] = nb1 - nb0;
+        c.acc = v3zero<T>();
+        c.sprev = 0.f;
+    }
+
+    // Element layer kk (between node planes kk and kk + 1), staged in ring slot kk % KU_RING;
+    // `n` is node (ie, je, kk). Stages layer kk + KU_DEPTH, writes node n when `emit`, and the
+    // carry of plane kk + 1 to `o`. `ep` holds node n's epilogue inputs, `epn` receives those
+    // of node n + plane.
+    __device__ __forceinline__ void step(int kk, int kend, bool emit, int64_t n, int par, const KuCarry<T>& in,
+                                         KuCarry<T>& o, const KuEpi<T>& ep, KuEpi<T>& epn, DotAcc<T>& dot) {
+        const int slot = kk & (KU_RING - 1);
+        issue_next(kend);
+        epi_load(n + plane, owner && kk + 1 < kend, epn);
+        V3<T> cu[2];
+        node_pair(slot, cu);
+        const float Ee = sm.E[slot][w][lane];
+        // edge differences of the upper plane
+        const V3<T> un0 = shfl_down3(cu[0]), un1 = shfl_down3(cu[1]);
+        o.dxb[0] = un0 - cu[0];
+        o.dxb[1] = un1 - cu[1];
+        o.dyb[0] = cu[1] - cu[0];
+        o.dyb[1] = un1 - un0;
+        V3<T> dz[2][2];
+        dz[0][0] = cu[0] - in.ub[0];
+        dz[0][1] = cu[1] - in.ub[1];
+        dz[1][0] = shfl_down3(dz[0][0]);
+        dz[1][1] = shfl_down3(dz[0][1]);
+        o.ub[0] = cu[0];
+        o.ub[1] = cu[1];
+
+        V3<T> f[2][2][2];
+        if (__any_sync(FULL, Ee != 0.f)) {
+            modal_element<T>(km, T(Ee), in.dxb, o.dxb, in.dyb, o.dyb, dz, f);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) (&f[0][0][0])[q] = v3zero<T>();
+        }
+        // x: corners px = 1 of lane l - 1 are corners px = 0 of lane l
+#pragma unroll
+        for (int py = 0; py < 2; ++py)
+#pragma unroll
+            for (int pz = 0; pz < 2; ++pz) f[0][py][pz] = f[0][py][pz] + shfl_up3(f[1][py][pz]);
+        float ex = 0.f;
+        if (MODE == KU_CHEB) ex = Ee + __shfl_up_sync(FULL, Ee, 1);
+        // y: corners py = 1 of warp w - 1 are corners py = 0 of warp w
+        T* xo = &sm.x[par][w + 1][0][lane];
+#pragma unroll
+        for (int pz = 0; pz < 2; ++pz) {
+            xo[(3 * pz) * 32] = f[0][1][pz].xy.x;
+            xo[(3 * pz + 1) * 32] = f[0][1][pz].xy.y;
+            xo[(3 * pz + 2) * 32] = f[0][1][pz].z;
+        }
+        if (MODE == KU_CHEB) xo[6 * 32] = T(ex);
+        cp_async_wait<KU_DEPTH - 1>();  // this thread's copies of layer kk + 1 have landed
+        __syncthreads();                // ... everyone's, and the y hand-over is visible
+        const T* xi = &sm.x[par][w][0][lane];
+#pragma unroll
+        for (int pz = 0; pz < 2; ++pz) {
+            V3<T> r;
+            r.xy.x = xi[(3 * pz) * 32];
+            r.xy.y = xi[(3 * pz + 1) * 32];
+            r.z = xi[(3 * pz + 2) * 32];
+            f[0][0][pz] = f[0][0][pz] + r;
+        }
+        if (MODE == KU_CHEB) ex += (float)xi[6 * 32];
+        o.acc = f[0][0][1];
+        o.sprev = ex;
+        if (emit && owner) {
+            const V3<T> yv = in.acc + f[0][0][0];
+            const T y[3] = {yv.xy.x, yv.xy.y, yv.z};
+            const T u[3] = {in.ub[0].xy.x, in.ub[0].xy.y, in.ub[0].z};
+            const uint8_t nm = ep.nm;
             if (MODE == KU_APPLY || MODE == KU_APPLY_DOT) {
+                T* yp = a.y + 3 * n;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const T v = (nm >> c) & 1 ? y[c] : T(0);
-                    a.y[3 * n + c] = v;
-                    if (MODE == KU_APPLY_DOT) dot.add(un[c], v);
+                    yp[c] = v;
+                    if (MODE == KU_APPLY_DOT) dot.add(u[c], v);
                 }
             } else if (MODE == KU_RESID) {
+                T* yp = a.y + 3 * n;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) a.y[3 * n + c] = (nm >> c) & 1 ? a.b[3 * n + c] - y[c] : T(0);
+                for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? ep.b[c] - y[c] : T(0);
             } else if (MODE == KU_CHEB) {
+                const float esum = in.sprev + ex;
                 const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
+                T* dp = a.dv + 3 * n;
+                T* xp = a.xout + 3 * n;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     T dn = T(0), xn = T(0);
                     if ((nm >> c) & 1) {
-                        const T rc = a.b[3 * n + c] - y[c];
-                        dn = (a.c1 != T(0) ? a.c1 * a.dv[3 * n + c] : T(0)) + a.c2 * rc * inv;
-                        xn = un[c] + dn;
+                        dn = a.c1 * ep.dv[c] + a.c2 * (ep.b[c] - y[c]) * inv;
+                        xn = u[c] + dn;
                     }
-                    a.dv[3 * n + c] = dn;
-                    a.xout[3 * n + c] = xn;
+                    dp[c] = dn;
+                    xp[c] = xn;
                 }
             }
         }
-        if (more) {
-            store_nodes(s_next);
-            store_elems(e_next);
-        }
+    }
+};
+
+// Work: the (node column tile, node plane) pairs, column-major, split into equal contiguous
+// ranges, one per CTA (a.kz planes each). A CTA walks its range as one or two z-segments of a
+// column tile; each segment recomputes the element layer below its first plane.
+template <class T, int MODE>
+__global__ void __launch_bounds__(KmCfg<T>::NT, KmCfg<T>::MINB) ku_kernel(KuArgs<T> a, KeModal<T> km) {
+    constexpr int NT = KmCfg<T>::NT;
+    using Tile = KuTile<T, MODE>;
+    extern __shared__ __align__(16) unsigned char ku_smem_raw[];
+    auto& sm = *reinterpret_cast<typename Tile::Smem*>(ku_smem_raw);
+    __shared__ double sred[NT / 32];
+    if (a.done != nullptr && *a.done) return;
+
+    Tile t(a, km, sm);
+    if (threadIdx.y == 0)  // the y hand-over row read by warp 0 stays zero
+        for (int q = 0; q < 2 * Tile::Smem::NV; ++q) sm.x[q / Tile::Smem::NV][0][q % Tile::Smem::NV][threadIdx.x] = T(0);
+    const int gx = ceil_div_d(t.NXn, KmCfg<T>::OX);
+    const int64_t total = (int64_t)gx * ceil_div_d(t.NYn, KmCfg<T>::OY) * t.NZn;
+    int64_t idx = (int64_t)blockIdx.x * a.kz;
+    const int64_t idx_end = min(total, idx + a.kz);
+    DotAcc<T> dot;
+    int par = 0;
+    while (idx < idx_end) {
+        const int64_t col = idx / t.NZn;
+        const int k0 = (int)(idx - col * t.NZn);
+        const int kend = (int)min((int64_t)t.NZn, (int64_t)k0 + (idx_end - idx));
+        idx += kend - k0;
+        t.set_column((int)(col % gx), (int)(col / gx), k0);
+        // prologue: layers k0-2 (its node plane k0-1 only) .. k0-2+KU_DEPTH in flight, one
+        // commit group each; step kk then stages layer kk+KU_DEPTH into the slot of kk-1
+#pragma unroll
+        for (int q = 0; q <= KU_DEPTH; ++q) t.issue_next(kend);
+        cp_async_wait<KU_DEPTH - 1>();  // layers k0-2 and k0-1 have landed
         __syncthreads();
+        KuCarry<T> A, B;
+        KuEpi<T> EA, EB;
+        t.start((k0 - 2) & (KU_RING - 1), A);
+        int64_t n = t.n0 + (int64_t)(k0 - 1) * t.plane;  // node (ie, je, kk)
+        t.epi_load(n, false, EA);
+        __syncthreads();  // slot of layer k0-2 is read before the loop refills it
+        for (int kk = k0 - 1; kk < kend; kk += 2) {
+            t.step(kk, kend, kk >= k0, n, par, A, B, EA, EB, dot);
+            par ^= 1;
+            n += t.plane;
+            if (kk + 1 >= kend) break;
+            t.step(kk + 1, kend, true, n, par, B, A, EB, EA, dot);
+            par ^= 1;
+            n += t.plane;
+        }
+        cp_async_wait<0>();
+        __syncthreads();  // the ring is idle before the next segment restages it
     }
     if (MODE == KU_APPLY_DOT) {
+        const int tid = threadIdx.y * 32 + threadIdx.x;
         double v[1] = {dot.value()};
-        block_sum<1, KU_NT>(v, sred, tid);
-        const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        finish_reduction<1, KU_NT>(v, bid, gridDim.x * gridDim.y * gridDim.z, a.partials, a.counter, a.red_out, tid,
-                                   sred);
+        block_sum<1, NT>(v, sred, tid);
+        finish_reduction<1, NT>(v, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sred);
     }
 }
 
-// z-chunking: the CTA count is a near multiple of the resident CTAs (occupancy x SMs), so
-// the last wave is full; chunks stay at least 4 layers deep (2 halo layers per chunk).
 template <class T, int MODE>
-static int ku_chunks(int columns, int NZn) {
+static int ku_resident() {
     static int resident = 0;
     if (resident == 0) {
         int dev = 0, sms = 1, occ = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ku_kernel<T, MODE>, KU_NT, 0);
+        const int bytes = (int)sizeof(KuSmem<T, MODE>);
+        cudaFuncSetAttribute(ku_kernel<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ku_kernel<T, MODE>, KmCfg<T>::NT, bytes);
         resident = std::max(1, sms * std::max(1, occ));
     }
-    int best = 1;
-    double best_score = -1.0;
-    for (int c = 1; c <= std::max(1, NZn / 4); ++c) {
-        const int kz = ceil_div(NZn, c);
-        const int64_t blocks = (int64_t)columns * ceil_div(NZn, kz);
-        const double waves = (double)blocks / resident;
-        const double eff = waves / std::ceil(waves);                 // last-wave fill
-        const double halo = (double)kz / (kz + 2);                    // halo-plane overhead
-        const double score = eff * halo * std::min(1.0, waves);        // need at least one wave
-        if (score > best_score + 1e-9) {
-            best_score = score;
-            best = c;
-        }
-    }
-    return best;
+    return resident;
 }
 
 // Evaluates the occupancy of every K u variant once (outside any stream capture).
 void ku_prepare() {
-    ku_chunks<float, KU_APPLY>(1, 8);
-    ku_chunks<float, KU_APPLY_DOT>(1, 8);
-    ku_chunks<float, KU_RESID>(1, 8);
-    ku_chunks<float, KU_CHEB>(1, 8);
-    ku_chunks<double, KU_APPLY>(1, 8);
-    ku_chunks<double, KU_APPLY_DOT>(1, 8);
-    ku_chunks<double, KU_RESID>(1, 8);
-    ku_chunks<double, KU_CHEB>(1, 8);
+    ku_resident<float, KU_APPLY>();
+    ku_resident<float, KU_APPLY_DOT>();
+    ku_resident<float, KU_RESID>();
+    ku_resident<float, KU_CHEB>();
+    ku_resident<double, KU_APPLY>();
+    ku_resident<double, KU_APPLY_DOT>();
+    ku_resident<double, KU_RESID>();
+    ku_resident<double, KU_CHEB>();
 }
 
 template <class T>
-int launch_ku(int mode, const KuArgs<T>& args, const KeBlocks<T>& kb, cudaStream_t s) {
+int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_t s) {
     KuArgs<T> a = args;
     const Dims& d = a.d;
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-    const int gx = ceil_div(NXn, KU_BX), gy = ceil_div(NYn, KU_BY);
-    int chunks = 1;
+    const int64_t total = (int64_t)ceil_div(NXn, KmCfg<T>::OX) * ceil_div(NYn, KmCfg<T>::OY) * NZn;
+    int resident = 1;
     switch (mode) {
-        case KU_APPLY: chunks = ku_chunks<T, KU_APPLY>(gx * gy, NZn); break;
-        case KU_APPLY_DOT: chunks = ku_chunks<T, KU_APPLY_DOT>(gx * gy, NZn); break;
-        case KU_RESID: chunks = ku_chunks<T, KU_RESID>(gx * gy, NZn); break;
-        case KU_CHEB: chunks = ku_chunks<T, KU_CHEB>(gx * gy, NZn); break;
+        case KU_APPLY: resident = ku_resident<T, KU_APPLY>(); break;
+        case KU_APPLY_DOT: resident = ku_resident<T, KU_APPLY_DOT>(); break;
+        case KU_RESID: resident = ku_resident<T, KU_RESID>(); break;
+        case KU_CHEB: resident = ku_resident<T, KU_CHEB>(); break;
         default: return ANL_ERR_BADARG;
     }
-    a.kz = ceil_div(NZn, chunks);
-    dim3 grid(gx, gy, ceil_div(NZn, a.kz));
-    dim3 block(KU_BX, KU_BY);
-    if (mode == KU_APPLY_DOT && (int64_t)grid.x * grid.y * grid.z > a.partial_capacity) {
-        set_error("K u dot: %d blocks exceed the reduction scratch (%d)", grid.x * grid.y * grid.z,
-                  a.partial_capacity);
+    // one wave of CTAs, at least 8 planes each (a segment costs one extra element layer)
+    a.kz = (int)std::max<int64_t>(8, (total + resident - 1) / resident);
+    const int blocks = (int)((total + a.kz - 1) / a.kz);
+    dim3 block(32, KmCfg<T>::NW);
+    if (mode == KU_APPLY_DOT && blocks > a.partial_capacity) {
+        set_error("K u dot: %d blocks exceed the reduction scratch (%d)", blocks, a.partial_capacity);
         return ANL_ERR_BADARG;
     }
     switch (mode) {
-        case KU_APPLY: ku_kernel<T, KU_APPLY><<<grid, block, 0, s>>>(a, kb); break;
-        case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<grid, block, 0, s>>>(a, kb); break;
-        case KU_RESID: ku_kernel<T, KU_RESID><<<grid, block, 0, s>>>(a, kb); break;
-        case KU_CHEB: ku_kernel<T, KU_CHEB><<<grid, block, 0, s>>>(a, kb); break;
+        case KU_APPLY: ku_kernel<T, KU_APPLY><<<blocks, block, sizeof(KuSmem<T, KU_APPLY>), s>>>(a, km); break;
+        case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<blocks, block, sizeof(KuSmem<T, KU_APPLY_DOT>), s>>>(a, km); break;
+        case KU_RESID: ku_kernel<T, KU_RESID><<<blocks, block, sizeof(KuSmem<T, KU_RESID>), s>>>(a, km); break;
+        case KU_CHEB: ku_kernel<T, KU_CHEB><<<blocks, block, sizeof(KuSmem<T, KU_CHEB>), s>>>(a, km); break;
         default: return ANL_ERR_BADARG;
     }
     ANL_LAUNCH_CHECK();
@@ -450,13 +625,18 @@ int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, cudaStre
     return ANL_OK;
 }
 
-// Upper bound of the K u grid (chunks of at least 4 layers): sizes the reduction scratch.
+// Upper bound of the K u grids (one CTA per SM and resident slot, at most 8 per SM) and of
+// the residual grid (chunks of 16 planes): sizes the reduction scratch.
 int ku_grid_blocks(const Dims& d) {
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-    return ceil_div(NXn, KU_BX) * ceil_div(NYn, KU_BY) * std::max(1, NZn / 4 + 1);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int bres = ceil_div(NXn, KU_BX) * ceil_div(NYn, KU_BY) * (ceil_div(NZn, 16) + 1);
+    return std::max(8 * sms, bres);
 }
 
-template int launch_ku<float>(int, const KuArgs<float>&, const KeBlocks<float>&, cudaStream_t);
-template int launch_ku<double>(int, const KuArgs<double>&, const KeBlocks<double>&, cudaStream_t);
+template int launch_ku<float>(int, const KuArgs<float>&, const KeModal<float>&, cudaStream_t);
+template int launch_ku<double>(int, const KuArgs<double>&, const KeModal<double>&, cudaStream_t);
 
 }  // namespace anl

@@ -555,11 +555,11 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
 // ------------------------------------------------------------------ host side
 
 template <class T>
-static KeBlocks<T> blocks_of(const anl_ctx* c);
+static KeModal<T> modal_of(const anl_ctx* c);
 template <>
-KeBlocks<float> blocks_of<float>(const anl_ctx* c) { return c->kbf; }
+KeModal<float> modal_of<float>(const anl_ctx* c) { return c->kmf; }
 template <>
-KeBlocks<double> blocks_of<double>(const anl_ctx* c) { return c->kbd; }
+KeModal<double> modal_of<double>(const anl_ctx* c) { return c->kmd; }
 
 template <class T>
 static KuArgs<T> ku_args(anl_ctx* c, const Level& L) {
@@ -582,7 +582,7 @@ static int apply_level(anl_ctx* c, const Level& L, const T* u, T* y, cudaStream_
     a.y = y;
     a.done = done;
     a.red_out = dot_out;
-    return launch_ku<T>(dot_out ? KU_APPLY_DOT : KU_APPLY, a, blocks_of<T>(c), s);
+    return launch_ku<T>(dot_out ? KU_APPLY_DOT : KU_APPLY, a, modal_of<T>(c), s);
 }
 
 // Largest eigenvalue of D^-1 K on a level: 15 power steps, then the Rayleigh quotient
@@ -695,7 +695,7 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
         a.c1 = T(cf[k].c1);
         a.c2 = T(cf[k].c2);
         a.done = done;
-        ANL_TRY(launch_ku<T>(KU_CHEB, a, blocks_of<T>(c), s));
+        ANL_TRY(launch_ku<T>(KU_CHEB, a, modal_of<T>(c), s));
         std::swap(L.x, L.xt);
     }
     return ANL_OK;
@@ -721,7 +721,7 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     a.b = (const T*)L.b;
     a.y = (T*)L.r;
     a.done = done;
-    ANL_TRY(launch_ku<T>(KU_RESID, a, blocks_of<T>(c), s));
+    ANL_TRY(launch_ku<T>(KU_RESID, a, modal_of<T>(c), s));
     k_restrict<T><<<vgrid(C.d.nn()), VT, 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<T>(c, l + 1, done, s));

@@ -38,7 +38,7 @@ def _ctx(shape, active, fixed, fp64, h=1.0, nu=0.3):
     return c
 
 
-@pytest.mark.parametrize("shape", [(7, 5, 4), (13, 7, 5), (40, 11, 19), (33, 9, 17)])
+@pytest.mark.parametrize("shape", [(7, 5, 4), (13, 7, 5), (40, 11, 19), (33, 9, 17), (61, 31, 23), (70, 33, 40)])
 @pytest.mark.parametrize("fp64", [False, True])
 def test_apply_K_matches_oracle(oracle, shape, fp64):
     active, fixed, E = _domain(shape, seed=sum(shape))
