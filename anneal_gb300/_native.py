@@ -30,6 +30,8 @@ EXPORTS = [
     "anl_sensitivity", "anl_stiffness_scale", "anl_filter_init", "anl_filter_fwd",
     "anl_filter_bwd", "anl_physical", "anl_oc_update", "anl_design_stats", "anl_profile_apply",
     "anl_launch_count", "anl_mg_info", "anl_dot_static",
+    "anl_mc_create", "anl_mc_destroy", "anl_mc_extract", "anl_mc_smooth", "anl_mc_components", "anl_mc_copy",
+    "anl_mc_table",
 ]
 
 
@@ -71,6 +73,13 @@ _SIGS = {
     "anl_launch_count": (I64, []),
     "anl_mg_info": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)]),
     "anl_dot_static": (I, [P, P, I64, P, P]),
+    "anl_mc_create": (I, [ctypes.POINTER(P)]),
+    "anl_mc_destroy": (None, [P]),
+    "anl_mc_extract": (I, [P, P, I, I, I, I, D, D, ctypes.POINTER(D), ctypes.POINTER(I64), ctypes.POINTER(I64), P]),
+    "anl_mc_smooth": (I, [P, I, D, D, P]),
+    "anl_mc_components": (I, [P, P, ctypes.POINTER(I), P]),
+    "anl_mc_copy": (I, [P, P, P, P]),
+    "anl_mc_table": (I, [P, P]),
 }
 
 

@@ -448,8 +448,9 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
         case KU_CHEB: resident = ku_resident<T, KU_CHEB>(); break;
         default: return ANL_ERR_BADARG;
     }
-    // one wave of CTAs, at least 8 planes each (a segment costs one extra element layer)
-    a.kz = (int)std::max<int64_t>(8, (total + resident - 1) / resident);
+    // one wave of CTAs. A segment costs one extra element layer, but a plane step is a
+    // ~1 us latency chain, so small (coarse-level) grids spread over many short segments.
+    a.kz = (int)std::max<int64_t>(2, (total + resident - 1) / resident);
     const int blocks = (int)((total + a.kz - 1) / a.kz);
     dim3 block(32, KmCfg<T>::NW);
     if (mode == KU_APPLY_DOT && blocks > a.partial_capacity) {

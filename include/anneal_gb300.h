@@ -148,6 +148,41 @@ int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const f
    nothing, frees nothing. */
 int anl_dot_static(const double* a, const double* b, int64_t n, double* out, anl_stream_t stream);
 
+/* ---------------------------------------------------------------- iso-surface export */
+
+/* An export workspace: device buffers that grow to the largest field seen, the derived
+   marching-cubes case table, and the last extracted mesh (float xyz vertices, int32 faces,
+   outward-facing, indexed: one vertex per crossed grid edge). Not thread-safe. */
+typedef struct anl_mc anl_mc;
+int anl_mc_create(anl_mc** out);
+void anl_mc_destroy(anl_mc* mc);
+
+/* Replaces export.surface (export.py:121-131): np.pad(f, 1), ndimage.zoom(order=1) by
+   `upsample`, measure.marching_cubes(level, spacing) and the shift origin - h/2.
+   field: nx*ny*nz element densities on the device (x fastest, grid.to3d order). Writes the
+   vertex and face counts (host). Samples (nx+2)(ny+2)(nz+2) upsample^3 must be <= 2^29. */
+int anl_mc_extract(anl_mc* mc, const float* field, int nx, int ny, int nz, int upsample, double level, double h,
+                   const double* origin_h, int64_t* nverts_h, int64_t* nfaces_h, anl_stream_t stream);
+
+/* Replaces trimesh.smoothing.filter_taubin (export.py:134): `iterations` umbrella steps
+   v += w (mean of neighbours - v), w = lamb on even steps and mu on odd ones (Taubin's
+   lambda|mu filter; the reference passes lamb 0.5, nu -0.53). */
+int anl_mc_smooth(anl_mc* mc, int iterations, double lamb, double mu, anl_stream_t stream);
+
+/* Replaces mesh.split (export.py:135): the connected component of every face, as the smallest
+   vertex index of the component (face_label: int32 per face, device). Writes the number of
+   hook-and-jump rounds to *rounds_h when it is not NULL. */
+int anl_mc_components(anl_mc* mc, int32_t* face_label, int* rounds_h, anl_stream_t stream);
+
+/* Copies the current mesh out: verts 3*nverts floats, faces 3*nfaces int32 (device or
+   pinned host pointers). */
+int anl_mc_copy(anl_mc* mc, float* verts, int32_t* faces, anl_stream_t stream);
+
+/* The derived case table (no counterpart in the reference, whose table lives in skimage):
+   ntri_h[256] triangles per cube case (bit c set when corner c = (x, y, z bits) is above the
+   level), tri_h[256*24] their cube edges (edge 4*axis + q, q the other two corner bits). */
+int anl_mc_table(uint8_t* ntri_h, int8_t* tri_h);
+
 /* ---------------------------------------------------------------- measurement */
 
 /* Multigrid hierarchy of the context (no counterpart in the reference): *nlev_h levels,
