@@ -1,6 +1,10 @@
 """Microbenchmark of the matrix-free K u kernel on a clamped box.
 
     python -m anneal_gb300.kernel_bench [--shape NX NY NZ] [--reps R] [--fp64]
+    python -m anneal_gb300.kernel_bench --export [--shape NX NY NZ] [--reps R]
+
+--export times the iso-surface export instead: zoom (x2), classify, scan, emit, 10 Taubin
+steps and the component labels on a smooth synthetic density field.
 
 Prints one JSON line: milliseconds per launch (CUDA events, after warm-up), the
 algorithmic bytes (24 per node + 4 per element: read u, write y, read the element
@@ -24,7 +28,10 @@ def main():
     ap.add_argument("--shape", type=int, nargs=3, default=[320, 160, 160])
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--export", action="store_true")
     a = ap.parse_args()
+    if a.export:
+        return export_bench(a.shape, a.reps)
     nx, ny, nz = a.shape
     ctx = Context((nx, ny, nz), 1.0, 0.3, fp64=a.fp64)
     ne, nn = ctx.ne, ctx.nn
@@ -46,6 +53,37 @@ def main():
                       "ms_per_launch": ms, "algorithmic_bytes": alg, "GBps": alg / (ms * 1e-3) / 1e9,
                       "tflops": MODAL_FLOPS * ne / (ms * 1e-3) / 1e12}))
     ctx.close()
+
+
+def export_bench(shape, reps):
+    """Iso-surface export of a lattice-like field (0.5 + 0.5 sin sin sin, period 16 voxels)."""
+    from . import export as X
+    nx, ny, nz = shape
+    i = torch.arange(nx, device="cuda", dtype=torch.float32)
+    j = torch.arange(ny, device="cuda", dtype=torch.float32)
+    k = torch.arange(nz, device="cuda", dtype=torch.float32)
+    w = 2 * np.pi / 16
+    f = 0.5 + 0.5 * (torch.sin(w * k)[:, None, None] * torch.sin(w * j)[None, :, None] * torch.sin(w * i)[None, None, :])
+    f = f.reshape(-1).contiguous()
+    mc = X.MarchingCubes()
+    res = {}
+    for phase in ("extract", "all"):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for r in range(reps + 2):
+            if r == 2:
+                e0.record()
+            nv, nf = mc.extract(f, shape, 0.5, 1.0, (0.0, 0.0, 0.0), 2)
+            if phase == "all":
+                mc.smooth(10)
+                mc.components()
+        e1.record()
+        e1.synchronize()
+        res[phase] = e0.elapsed_time(e1) / reps
+    mc.close()
+    ns = (nx + 2) * (ny + 2) * (nz + 2) * 8
+    print(json.dumps({"kernel": "iso-surface export", "shape": [nx, ny, nz], "upsample": 2, "samples": ns,
+                      "vertices": nv, "faces": nf, "ms_extract": res["extract"], "ms_with_smooth_and_labels": res["all"],
+                      "samples_per_s": ns / (res["extract"] * 1e-3)}))
 
 
 if __name__ == "__main__":

@@ -198,7 +198,7 @@ def taubin(verts, faces, iterations, lamb=0.5, mu=-0.53):
     nv = v.shape[0]
     a = np.concatenate([faces[:, 0], faces[:, 1], faces[:, 2]])
     b = np.concatenate([faces[:, 1], faces[:, 2], faces[:, 0]])
-    A = coo_matrix((np.ones(a.size), (np.concatenate([a, b]), np.concatenate([b, a]))), shape=(nv, nv)).tocsr()
+    A = coo_matrix((np.ones(2 * a.size), (np.concatenate([a, b]), np.concatenate([b, a]))), shape=(nv, nv)).tocsr()
     A.data[:] = 1.0
     deg = np.asarray(A.sum(axis=1)).ravel()
     for it in range(iterations):
