@@ -31,7 +31,8 @@ EXPORTS = [
     "anl_filter_bwd", "anl_physical", "anl_oc_update", "anl_design_stats", "anl_profile_apply",
     "anl_launch_count", "anl_mg_info", "anl_dot_static",
     "anl_mc_create", "anl_mc_destroy", "anl_mc_extract", "anl_mc_smooth", "anl_mc_components", "anl_mc_copy",
-    "anl_mc_table",
+    "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
+    "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam",
 ]
 
 
@@ -80,6 +81,14 @@ _SIGS = {
     "anl_mc_components": (I, [P, P, ctypes.POINTER(I), P]),
     "anl_mc_copy": (I, [P, P, P, P]),
     "anl_mc_table": (I, [P, P]),
+    "anl_nn_conv3d": (I, [P, P, P, P, P, I, I, I, I, I, I, I, I, P]),
+    "anl_nn_conv3d_bwd_data": (I, [P, P, P, P, I, I, I, I, I, I, I, P]),
+    "anl_nn_conv3d_bwd_weight": (I, [P, P, P, I64, P, P, I, I, I, I, I, I, I, P]),
+    "anl_nn_gelu_bwd": (I, [P, P, P, I64, P]),
+    "anl_nn_pool2": (I, [P, P, I, I, I, I, I, I, P]),
+    "anl_nn_up2": (I, [P, P, I, I, I, I, I, P]),
+    "anl_nn_mse": (I, [P, P, P, P, I, I64, P, P, P, P]),
+    "anl_nn_adam": (I, [P, P, P, P, I64, D, D, D, D, I, P]),
 }
 
 

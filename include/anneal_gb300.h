@@ -183,6 +183,42 @@ int anl_mc_copy(anl_mc* mc, float* verts, int32_t* faces, anl_stream_t stream);
    level), tri_h[256*24] their cube edges (edge 4*axis + q, q the other two corner bits). */
 int anl_mc_table(uint8_t* ntri_h, int8_t* tri_h);
 
+/* ---------------------------------------------------------------- warm-start network layers
+
+   No counterpart in the reference: the reference starts each solve from the previous
+   iterate (optimize.py:122); these kernels train and run the network that predicts a better
+   start. Tensors are one sample, [C][D][H][W] float with W fastest; weights [cout][cin][k^3]. */
+
+/* z = conv3d(x, w) + b (k = 1 or 3, zero padding k/2, stride 1; b may be NULL); a = GELU(z)
+   when act != 0. accumulate != 0 adds to z instead of overwriting it. */
+int anl_nn_conv3d(const float* x, const float* w, const float* b, float* z, float* a, int cin, int cout, int D,
+                  int H, int W, int ksize, int act, int accumulate, anl_stream_t stream);
+/* dx = conv3d^T(dz, w) (the gradient with respect to x); wt_work holds cin*cout*k^3 floats. */
+int anl_nn_conv3d_bwd_data(const float* dz, const float* w, float* wt_work, float* dx, int cin, int cout, int D,
+                           int H, int W, int ksize, int accumulate, anl_stream_t stream);
+/* dw, db (gradients with respect to w and b), summed over voxel chunks in a fixed order;
+   part_work holds part_floats >= cout*cin*k^3 + cout floats (more allows more chunks). */
+int anl_nn_conv3d_bwd_weight(const float* x, const float* dz, float* part_work, int64_t part_floats, float* dw,
+                             float* db, int cin, int cout, int D, int H, int W, int ksize, int accumulate,
+                             anl_stream_t stream);
+/* dz = da * GELU'(z) (erf form). */
+int anl_nn_gelu_bwd(const float* z, const float* da, float* dz, int64_t n, anl_stream_t stream);
+/* 2x average pooling of C channels of an even D x H x W grid; backward = 1 maps the pooled
+   gradient x to the full-size gradient y (added to y when accumulate != 0). */
+int anl_nn_pool2(const float* x, float* y, int C, int D, int H, int W, int backward, int accumulate,
+                 anl_stream_t stream);
+/* 2x nearest upsampling to an even D x H x W grid; backward = 1 sums the full-size gradient x
+   into the half-size gradient y. */
+int anl_nn_up2(const float* x, float* y, int C, int D, int H, int W, int backward, anl_stream_t stream);
+/* Masked mean-squared error over C channels sharing a per-voxel mask: out2[0] = sum m (y-t)^2,
+   out2[1] = sum m (device), dy = 2 m (y - t) / max(1, sum m). work: 2*1216 doubles; counter:
+   a zeroed unsigned (left zero). */
+int anl_nn_mse(const float* y, const float* tgt, const float* mask, float* dy, int C, int64_t vol, double* work,
+               unsigned* counter, double* out2, anl_stream_t stream);
+/* One Adam step (bias-corrected, step >= 1) on n FP32 parameters. */
+int anl_nn_adam(float* p, const float* g, float* m, float* v, int64_t n, double lr, double b1, double b2, double eps,
+                int step, anl_stream_t stream);
+
 /* ---------------------------------------------------------------- measurement */
 
 /* Multigrid hierarchy of the context (no counterpart in the reference): *nlev_h levels,
