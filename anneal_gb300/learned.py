@@ -303,12 +303,15 @@ def unpad_displacement(shape, y, dims):
 
 # -------------------------------------------------------------------- warm start
 
-def galerkin_start(ctx, escale, F, u_prev, u_net, free):
+def galerkin_start(ctx, escale, F, u_prev, u_net, free, with_gain=False):
     """x0 = a u_prev + b u_net minimising the energy error over the two directions.
-    free: (3 nn,) float64 0/1 mask. Returns (x0, a, b)."""
+    free: (3 nn,) float64 0/1 mask. Returns (x0, a, b), plus with ``with_gain`` the drop of
+    the energy Pi(x) = x.Kx/2 - F.x from the previous iterate to x0, relative to |Pi(u_prev)|
+    (Pi - Pi(u*) is half the squared energy error, so this is the share of it removed)."""
     vecs = [v * free for v in (u_prev, u_net) if v is not None and float(v.abs().max()) > 0]
     if not vecs:
-        return torch.zeros_like(F), 0.0, 0.0
+        z = torch.zeros_like(F)
+        return (z, 0.0, 0.0, 0.0) if with_gain else (z, 0.0, 0.0)
     Kv = []
     for v in vecs:
         y = torch.empty(v.numel(), dtype=F32, device="cuda")
@@ -324,9 +327,22 @@ def galerkin_start(ctx, escale, F, u_prev, u_net, free):
         c = np.zeros(n)
     x0 = sum(ci * v for ci, v in zip(c, vecs))
     coef = list(c) + [0.0] * (2 - n)
-    if u_prev is None or float(u_prev.abs().max()) == 0:
+    prev_ok = u_prev is not None and float(u_prev.abs().max()) > 0
+    if not prev_ok:
         coef = [0.0, coef[0]]
-    return x0, coef[0], coef[1]
+    if not with_gain:
+        return x0, coef[0], coef[1]
+    pi0 = 0.5 * G[0, 0] - rhs[0] if prev_ok else 0.0
+    pi1 = -0.5 * float(c @ rhs)
+    gain = (pi0 - pi1) / abs(pi0) if prev_ok and pi0 != 0 else 1.0
+    return x0, coef[0], coef[1], gain
+
+
+def energy(ctx, escale, F, x):
+    """Pi(x) = x.Kx / 2 - F.x with the FP32 operator (one K u)."""
+    y = torch.empty(x.numel(), dtype=F32, device="cuda")
+    ctx.apply_K(escale, x.float().contiguous(), y)
+    return 0.5 * float(x @ y.double()) - float(F @ x)
 
 
 class WarmStart:

@@ -67,7 +67,7 @@ class SimpRunner:
 
     def __init__(self, grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=80, r_mm=None,
                  p_final=3.0, move=0.2, combine="sum", log=print, x0=None, beta_max=BETA_MAX, rtol=None,
-                 maxiter=2000):
+                 maxiter=2000, warm_start=None):
         self.grid = grid
         self.E0, self.vf, self.iters, self.p_final, self.move = float(E0), float(vf), int(iters), p_final, move
         self.combine, self.log, self.beta_max, self.maxiter = combine, log, beta_max, maxiter
@@ -130,6 +130,16 @@ class SimpRunner:
         self.it = 0
         self.hist = []
         self.p = 1.0
+        # optional learned start (anneal_gb300.learned.WarmStart); dropped once its Galerkin
+        # combination stops lowering the energy of the previous iterate
+        self.warm_start = warm_start
+        self.ws_gain = []
+        self.ws_judge = []
+        if warm_start is not None:
+            fx = torch.zeros(3 * grid.nnode, dtype=torch.uint8, device="cuda")
+            fx[torch.as_tensor(np.asarray(fixed, np.int64), device="cuda")] = 1
+            self._ws_fixed = fx
+            self._ws_free = fem._mask_t.to(torch.uint8)
 
     def step(self):
         """One SIMP iteration (optimize.py:105-172); returns its history record."""
@@ -149,7 +159,11 @@ class SimpRunner:
         ctx.stiffness_scale(self.xphys_t, self.phi_t, self.E0, self.emin, p, self.escale_t)
         last = fem.cg_iters[-1] if fem.cg_iters else None
         rebuild = self.base_iters is None or (last is not None and last > 1.6 * self.base_iters)
+        ws = self._learned_start() if self.warm_start is not None else None
+        t_solve = time.perf_counter()
         fem.solve_device(self.escale_t, self.F_t, self.U_t, rtol=self.rtol, maxiter=self.maxiter, rebuild=rebuild)
+        if ws is not None:
+            self._judge_learned_start(ws, time.perf_counter() - t_solve)
         if rebuild:
             self.base_iters = fem.cg_iters[-1]
         nc = len(self.cases)
@@ -182,6 +196,52 @@ class SimpRunner:
                  f"change {change:.3f}  grey {grey:.2f}  cg {fem.cg_iters[-1]}{' amg' if rebuild else ''}  "
                  f"{rec['seconds']:.1f}s")
         return rec
+
+    def _learned_start(self):
+        """Replaces each case's start by the energy-optimal combination of the previous
+        iterate and the network's prediction (anneal_gb300.learned.galerkin_start). Returns
+        what the judgement after the solve needs."""
+        from . import learned as LW
+        ctx = self.ctx
+        free = self._ws_free.double()
+        t0 = time.perf_counter()
+        info = []
+        for c in range(len(self.cases)):
+            F = self.F_t[c]
+            u_prev = self.U_t[c].clone()
+            u_net = self.warm_start.predict(self.escale_t, F, self._ws_fixed, self._ws_free)
+            x0, a, b, gain = LW.galerkin_start(ctx, self.escale_t, F, u_prev, u_net, free, with_gain=True)
+            info.append((LW.energy(ctx, self.escale_t, F, u_prev), LW.energy(ctx, self.escale_t, F, x0)))
+            self.U_t[c].copy_(x0)
+            self.ws_gain.append(gain)
+        torch.cuda.synchronize()
+        return info, time.perf_counter() - t0
+
+    def _judge_learned_start(self, ws, t_solve):
+        """After the solve, Pi(u) = u.Ku/2 - F.u of the solution gives the initial energy
+        errors of both starts (Pi(x) - Pi(u*) = |x - u*|_K^2 / 2). CG needs iterations in
+        proportion to log(initial / final energy error), the final one being about
+        rtol^2 |Pi(u*)|, so the previous iterate would have needed about
+        it * log(e_prev / e_fin) / log(e_new / e_fin) iterations. The network is dropped after
+        two SIMP iterations in a row where the saved iterations cost less than the prediction."""
+        from . import learned as LW
+        info, t_pred = ws
+        nc = len(self.cases)
+        its = self.fem.cg_iters[-nc:]
+        saved_s = 0.0
+        for c in range(nc):
+            pi_star = LW.energy(self.ctx, self.escale_t, self.F_t[c], self.U_t[c])
+            e_fin = max(self.rtol ** 2 * abs(pi_star), 1e-300)
+            e_prev = max(info[c][0] - pi_star, e_fin)
+            e_new = max(info[c][1] - pi_star, e_fin)
+            it = max(its[c], 1)
+            if e_new > e_fin:
+                would = it * np.log(e_prev / e_fin) / np.log(e_new / e_fin)
+                saved_s += max(0.0, would - it) * t_solve / (nc * it)
+        self.ws_judge.append((saved_s, t_pred))
+        recent = self.ws_judge[-2:]
+        if len(recent) == 2 and all(sv < tp for sv, tp in recent):
+            self.warm_start = None
 
     def step_host(self, x_in, x_out):
         """One iteration with the design exchanged through host memory: x_in (host float32,
