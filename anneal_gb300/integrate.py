@@ -5,9 +5,10 @@
 
 ``install`` swaps the reference's solve and optimise entry points for the GPU ones in the
 already imported (or importable) ``anneal`` package: ``anneal.fem.FEM`` / ``SolverError``,
-``anneal.optimize.simp`` / ``Filter``, the names ``run.py`` bound at import
-(``anneal.run.FEM``, ``anneal.run.simp``) and the validation gate's checks. Spec parsing,
-exports, reports and the database stay the reference's.
+``anneal.optimize.simp`` / ``Filter``, ``anneal.export.surface``, the names ``run.py`` bound
+at import (``anneal.run.FEM``, ``anneal.run.simp``, ``anneal.run.surface``) and the validation
+gate's checks. Spec parsing, the other export steps, reports and the database stay the
+reference's.
 """
 import importlib
 
@@ -25,10 +26,17 @@ def install(anneal_pkg="anneal"):
     opt.simp = gopt.simp
     opt.Filter = gopt.Filter
     opt.benchmark_cantilever = gopt.benchmark_cantilever
+    from . import export as gexp
+    try:
+        exp = importlib.import_module(f"{anneal_pkg}.export")
+        exp.surface = gexp.surface
+    except ImportError:   # export.py needs trimesh / skimage
+        pass
     try:
         run = importlib.import_module(f"{anneal_pkg}.run")
         run.FEM = gfem.FEM
         run.simp = gopt.simp
+        run.surface = gexp.surface
     except ImportError:   # run.py needs trimesh / skimage / matplotlib
         pass
     try:
