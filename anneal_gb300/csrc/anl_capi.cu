@@ -7,6 +7,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "anl_ctx.cuh"
 
@@ -155,6 +156,8 @@ double ke_modal(const double* ke, KeModal<double>* out) {
 
 // ------------------------------------------------------------------ declarations from other units
 
+void cheb_coefficients(double bound, int degree, double* out);
+
 int solver_setup_domain(anl_ctx* c, const uint8_t* active, const uint8_t* fixed, cudaStream_t s);
 int solver_apply(anl_ctx* c, const float* escale, const void* u, void* y, cudaStream_t s);
 int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, int nrhs, double rtol, int maxiter,
@@ -180,6 +183,18 @@ int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* m
 
 // ------------------------------------------------------------------ context
 
+// the smoother's coefficients for every level (the last one, when it is not solved densely,
+// gets a 16-step sweep)
+static cudaError_t upload_cheb(anl_ctx* c) {
+    std::vector<double> h(c->lev.size() * kChebStride, 0.0);
+    for (size_t l = 0; l < c->lev.size(); ++l) {
+        const bool last = l + 1 == c->lev.size();
+        cheb_coefficients(c->lmax_bound, last ? 16 : c->mg_degree, h.data() + l * kChebStride);
+        c->lev[l].lmax = c->lmax_bound;
+    }
+    return cudaMemcpy(c->cheb_d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+}
+
 static void free_ctx(anl_ctx* c) {
     if (!c) return;
     auto f = [](void* p) {
@@ -197,6 +212,7 @@ static void free_ctx(anl_ctx* c) {
         f(L.dv);
     }
     f(c->ke_d);
+    f(c->cheb_d);
     f(c->active);
     f(c->A);
     f(c->Ainv);
@@ -257,6 +273,28 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     c->kmf = KeModal<float>{(float)c->kmd.ab, (float)c->kmd.b, (float)c->kmd.c,  (float)c->kmd.d,
                             (float)c->kmd.f,  (float)c->kmd.gh, (float)c->kmd.h, (float)c->kmd.j};
     c->kdiag = c->ke[0];
+    {  // largest eigenvalue of Ke by power iteration in FP64 (Ke is positive semidefinite)
+        double v[24], w[24], lam = 0.0;
+        for (int i = 0; i < 24; ++i) v[i] = 1.0 + 0.01 * i * (i % 3 + 1);
+        for (int it = 0; it < 3000; ++it) {
+            double nrm = 0.0;
+            for (int i = 0; i < 24; ++i) {
+                double sacc = 0.0;
+                for (int j = 0; j < 24; ++j) sacc += c->ke[i * 24 + j] * v[j];
+                w[i] = sacc;
+                nrm += sacc * sacc;
+            }
+            nrm = std::sqrt(nrm);
+            double vw = 0.0, vv = 0.0;
+            for (int i = 0; i < 24; ++i) {
+                vw += v[i] * w[i];
+                vv += v[i] * v[i];
+            }
+            lam = vw / vv;
+            for (int i = 0; i < 24; ++i) v[i] = w[i] / nrm;
+        }
+        c->lmax_bound = 1.001 * lam / c->kdiag;
+    }
 
 #define ALLOC(ptr, bytes)                                                  \
     do {                                                                   \
@@ -299,6 +337,7 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         ALLOC(c->Ainv, (size_t)c->nc * c->nc * sizeof(double));
     }
     ALLOC(c->flag_d, 4 * sizeof(int));
+    ALLOC(c->cheb_d, c->lev.size() * kChebStride * sizeof(double));
     ALLOC(c->ke_d, 576 * sizeof(double));
     if (cudaMemcpy(c->ke_d, c->ke, 576 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
         set_error("copy of the element matrix failed");
@@ -344,6 +383,7 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         return ANL_ERR_NOMEM;
     }
     if (cudaMemset(c->counter, 0, 16 * sizeof(unsigned)) != cudaSuccess ||
+        upload_cheb(c) != cudaSuccess ||
         cudaMemset(c->flag_d, 0, 4 * sizeof(int)) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
         set_error("context initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
         free_ctx(c);

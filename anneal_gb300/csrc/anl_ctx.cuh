@@ -21,7 +21,7 @@ struct Level {
     void* b = nullptr;        // right-hand side (level 0: the CG residual r)
     void* r = nullptr;        // residual scratch
     void* dv = nullptr;       // Chebyshev direction
-    double lmax = 0.0;        // largest eigenvalue estimate of D^-1 K
+    double lmax = 0.0;        // upper end of the smoothed spectrum of D^-1 K (diagnostics)
 };
 
 struct FilterState {
@@ -33,6 +33,8 @@ struct FilterState {
 };
 
 constexpr int kMaxFilterR = 5;
+constexpr int kChebMax = 32;
+constexpr int kChebStride = 1 + 2 * kChebMax;
 
 }  // namespace anl
 
@@ -50,12 +52,21 @@ struct anl_ctx {
     anl::KeModal<double> kmd{};
     anl::KeModal<float> kmf{};
     double kdiag = 0.0;
+    // lambda_max(Ke) / Ke_00 >= lambda_max(D^-1 K) for every field of element scales (the
+    // element-by-element bound: x.Kx = sum_e E_e x_e.Ke x_e <= bound sum_e E_e Ke_00 |x_e|^2)
+    double lmax_bound = 0.0;
 
     bool domain_set = false;
     int64_t nfree = 0;
     uint8_t* active = nullptr;      // level-0 active flags (ne)
     std::vector<anl::Level> lev;
-    int mg_degree = 2;
+#ifndef ANL_MG_DEGREE
+#define ANL_MG_DEGREE 2  // Chebyshev steps per pre- and post-smoothing
+#endif
+    int mg_degree = ANL_MG_DEGREE;
+    // per level: {lambda_max bound, then (c1, c2) for up to kChebMax steps}, read by the
+    // smoothing kernels from device memory
+    double* cheb_d = nullptr;
 
     // coarsest level: dense factor (FP64) or a Chebyshev fallback when too large
     int nc = 0;

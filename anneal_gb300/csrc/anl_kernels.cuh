@@ -21,6 +21,8 @@ struct KuArgs {
     T* dv = nullptr;                 // CHEB: Chebyshev direction, updated in place
     T* xout = nullptr;               // CHEB: u + new direction
     T c1 = T(0), c2 = T(0);          // CHEB: d <- c1 d + c2 D^-1 (b - K u)
+    const double* cheb = nullptr;    // CHEB: {c1, c2} in device memory (overrides c1, c2)
+    int c1_zero = 0;                 // CHEB: first step of a sweep (c1 = 0, d is not read)
     T kdiag = T(0);                  // diagonal entry of Ke(1) (all 24 are equal)
     double* partials = nullptr;      // APPLY_DOT reduction scratch
     unsigned* counter = nullptr;

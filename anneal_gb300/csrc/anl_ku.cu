@@ -231,7 +231,7 @@ struct KuTile {
             }
             if (MODE == KU_CHEB) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) e.dv[c] = a.c1 != T(0) ? a.dv[3 * n + c] : T(0);
+                for (int c = 0; c < 3; ++c) e.dv[c] = a.c1_zero ? T(0) : a.dv[3 * n + c];
             }
         }
     }
@@ -331,13 +331,14 @@ struct KuTile {
             } else if (MODE == KU_CHEB) {
                 const float esum = in.sprev + ex;
                 const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
+                const T c1 = a.cheb ? T(a.cheb[0]) : a.c1, c2 = a.cheb ? T(a.cheb[1]) : a.c2;
                 T* dp = a.dv + 3 * n;
                 T* xp = a.xout + 3 * n;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     T dn = T(0), xn = T(0);
                     if ((nm >> c) & 1) {
-                        dn = a.c1 * ep.dv[c] + a.c2 * (ep.b[c] - y[c]) * inv;
+                        dn = c1 * ep.dv[c] + c2 * (ep.b[c] - y[c]) * inv;
                         xn = u[c] + dn;
                     }
                     dp[c] = dn;

@@ -5,9 +5,10 @@
 //  * the operator is the matrix-free K u of anl_ku.cu (FP32, or FP64 with ANL_FLAG_FP64);
 //  * the preconditioner is a V-cycle on the voxel hierarchy (element dims halved per level):
 //    coarse element scale = (sum of the 8 children)/4 (their mean at Ke(2h) = 2 Ke(h)),
-//    trilinear prolongation P and restriction P^T, Chebyshev smoothing on D^-1 K with the
-//    spectrum bound from power iteration, and a dense FP64 Cholesky solve on the coarsest
-//    grid (a high-degree Chebyshev sweep if that grid is too large for a dense factor);
+//    trilinear prolongation P and restriction P^T, Chebyshev smoothing on D^-1 K over
+//    [0.05, 1] x the element bound lambda_max(Ke) / Ke_00 (an upper bound of the spectrum for
+//    every design), and a dense FP64 Cholesky solve on the coarsest grid, refactored every
+//    solve (a high-degree Chebyshev sweep if that grid is too large for a dense factor);
 //  * the CG iterate x and right-hand side stay in FP64; the CG scalars come from FP64
 //    reductions (compensated FP32 partials); the residual is replaced by the true
 //    residual b - K x (x split as hi + lo in FP32) periodically and before convergence is
@@ -215,9 +216,10 @@ __global__ void k_prolong_add(Dims f, Dims c, const T* xc, const uint8_t* nmf, T
 
 // x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
 template <class T>
-__global__ void k_cheb_first(int64_t nn, const T* b, const float* diag, const uint8_t* nmask, T c2, T* x, T* dv,
-                             const int* done) {
+__global__ void k_cheb_first(int64_t nn, const T* b, const float* diag, const uint8_t* nmask, const double* c2p, T* x,
+                             T* dv, const int* done) {
     if (done && *done) return;
+    const T c2 = T(*c2p);
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
         const uint8_t m = nmask[n];
         const float dg = diag[n];
@@ -228,47 +230,6 @@ __global__ void k_cheb_first(int64_t nn, const T* b, const float* diag, const ui
             dv[3 * n + c] = v;
         }
     }
-}
-
-// ------------------------------------------------------------------ power iteration
-
-__device__ __forceinline__ float hash01(uint64_t i) {
-    uint64_t z = i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    z ^= z >> 31;
-    return (float)((z >> 40) * (1.0 / 16777216.0));
-}
-
-template <class T>
-__global__ void k_power_init(int64_t nn, const uint8_t* nmask, T* v) {
-    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t m = nmask[n];
-        for (int c = 0; c < 3; ++c) v[3 * n + c] = (m >> c) & 1 ? T(0.5f + hash01(3 * n + c)) : T(0);
-    }
-}
-
-// v = D^-1 y, rescaled by 1/scale to keep magnitudes near one
-template <class T>
-__global__ void k_jacobi_scale(int64_t nn, const T* y, const float* diag, const uint8_t* nmask, T scale, T* v) {
-    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t m = nmask[n];
-        const float dg = diag[n];
-        for (int c = 0; c < 3; ++c) v[3 * n + c] = ((m >> c) & 1) && dg > 0.f ? y[3 * n + c] / (T(dg) * scale) : T(0);
-    }
-}
-
-template <class T>
-__global__ void k_dot_diag(int64_t nn, const T* v, const float* diag, double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[VT / 32];
-    Sum<T> s;
-    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
-        const T dg = T(diag[n]);
-        for (int c = 0; c < 3; ++c) s.prod(v[3 * n + c] * dg, v[3 * n + c]);
-    }
-    double val[1] = {s.get()};
-    block_sum<1, VT>(val, sm, threadIdx.x);
-    finish_reduction<1, VT>(val, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 // ------------------------------------------------------------------ coarsest grid (FP64)
@@ -585,30 +546,30 @@ static int apply_level(anl_ctx* c, const Level& L, const T* u, T* y, cudaStream_
     return launch_ku<T>(dot_out ? KU_APPLY_DOT : KU_APPLY, a, modal_of<T>(c), s);
 }
 
-// Largest eigenvalue of D^-1 K on a level: 15 power steps, then the Rayleigh quotient
-// v.Kv / v.Dv. The estimate approaches lambda_max from below (measured 0.9-0.97 of it).
-template <class T>
-static int estimate_lmax(anl_ctx* c, Level& L, cudaStream_t s) {
-    const int64_t nn = L.d.nn();
-    T* v = (T*)L.x;
-    T* y = (T*)L.r;
-    k_power_init<T><<<vgrid(nn), VT, 0, s>>>(nn, L.nmask, v);
-    ANL_LAUNCH_CHECK();
-    double scale = 1.0;
-    for (int it = 0; it < 15; ++it) {
-        ANL_TRY(apply_level<T>(c, L, v, y, s));
-        k_jacobi_scale<T><<<vgrid(nn), VT, 0, s>>>(nn, y, L.diag, L.nmask, T(scale), v);
-        ANL_LAUNCH_CHECK();
-        scale = 3.0;  // typical growth per step; keeps values O(1)
+static int level_index(const anl_ctx* c, const Level& L) { return (int)(&L - &c->lev[0]); }
+
+#ifndef ANL_CHEB_LO
+#define ANL_CHEB_LO 0.05  // lower end of the smoothed interval, as a fraction of its upper end
+#endif
+
+// Chebyshev coefficients of a `degree`-step sweep of D^-1 K over [ANL_CHEB_LO, 1] x bound,
+// where bound = lambda_max(Ke) / Ke_00 >= lambda_max(D^-1 K) on every level and for every
+// design: out = {bound, c1_0, c2_0, c1_1, c2_1, ...}. A power-iteration estimate of the
+// spectrum approaches lambda_max from below and misses the localised top modes of solid
+// voxels inside void, which a sweep above its interval amplifies; the bound cannot.
+void cheb_coefficients(double bound, int degree, double* out) {
+    const double hi = bound, lo = ANL_CHEB_LO * bound;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    double rho_old = 1.0 / sigma;
+    out[0] = bound;
+    out[1] = 0.0;
+    out[2] = 1.0 / theta;
+    for (int k = 1; k < degree && k < kChebMax; ++k) {
+        const double rho = 1.0 / (2.0 * sigma - rho_old);
+        out[1 + 2 * k] = rho * rho_old;
+        out[2 + 2 * k] = 2.0 * rho / delta;
+        rho_old = rho;
     }
-    ANL_TRY(apply_level<T>(c, L, v, y, s, c->red_out));
-    k_dot_diag<T><<<vgrid(nn), VT, 0, s>>>(nn, v, L.diag, c->partials, c->counter, c->red_out + 1);
-    ANL_LAUNCH_CHECK();
-    ANL_CUDA(cudaMemcpyAsync(c->red_h, c->red_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    ANL_CUDA(cudaStreamSynchronize(s));
-    const double num = c->red_h[0], den = c->red_h[1];
-    L.lmax = (den > 0 && std::isfinite(num / den) && num > 0) ? num / den : 4.0;
-    return ANL_OK;
 }
 
 static int coarse_factor(anl_ctx* c, cudaStream_t s) {
@@ -647,42 +608,23 @@ static int update_hierarchy(anl_ctx* c, bool rebuild, cudaStream_t s) {
         k_diag<<<vgrid(L.d.nn()), VT, 0, s>>>(L.d, L.E, (float)c->kdiag, L.diag);
         ANL_LAUNCH_CHECK();
     }
-    const bool first = !c->coarse_ready;
-    if (rebuild || first) {
-        c->cg_valid = false;  // the Chebyshev coefficients in the captured graph change
-        const size_t nsm = c->dense_coarse ? c->lev.size() - 1 : c->lev.size();
-        for (size_t l = 0; l < nsm; ++l) ANL_TRY(estimate_lmax<T>(c, c->lev[l], s));
-        if (c->dense_coarse) ANL_TRY(coarse_factor(c, s));
-        else c->coarse_ready = true;
-    }
+    // the coarsest grid's factor follows the design every solve: a stale one makes the
+    // V-cycle a poor (even indefinite) preconditioner once the design has moved on
+    (void)rebuild;
+    if (c->dense_coarse) ANL_TRY(coarse_factor(c, s));
+    else c->coarse_ready = true;
     return ANL_OK;
 }
 
-struct ChebCoef {
-    double c1, c2;
-};
-
-static void cheb_coefs(double lmax, int degree, ChebCoef* out) {
-    const double hi = 1.1 * lmax, lo = 0.1 * lmax;
-    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
-    double rho_old = 1.0 / sigma;
-    out[0] = {0.0, 1.0 / theta};
-    for (int k = 1; k < degree; ++k) {
-        const double rho = 1.0 / (2.0 * sigma - rho_old);
-        out[k] = {rho * rho_old, 2.0 * rho / delta};
-        rho_old = rho;
-    }
-}
-
-// degree Chebyshev steps on level L; x_is_zero uses the elementwise first step.
+// degree Chebyshev steps on level L with the device coefficients of that level; x_is_zero
+// uses the elementwise first step.
 template <class T>
 static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* done, cudaStream_t s) {
-    ChebCoef cf[32];
-    cheb_coefs(L.lmax, degree, cf);
+    const double* cf = c->cheb_d + (size_t)level_index(c, L) * kChebStride + 1;  // (c1, c2) pairs
     int k0 = 0;
     if (x_is_zero) {
-        k_cheb_first<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const T*)L.b, L.diag, L.nmask, T(cf[0].c2),
-                                                         (T*)L.x, (T*)L.dv, done);
+        k_cheb_first<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const T*)L.b, L.diag, L.nmask, cf + 1, (T*)L.x,
+                                                         (T*)L.dv, done);
         ANL_LAUNCH_CHECK();
         k0 = 1;
     }
@@ -692,8 +634,8 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
         a.b = (const T*)L.b;
         a.dv = (T*)L.dv;
         a.xout = (T*)L.xt;
-        a.c1 = T(cf[k].c1);
-        a.c2 = T(cf[k].c2);
+        a.cheb = cf + 2 * k;
+        a.c1_zero = k == 0;
         a.done = done;
         ANL_TRY(launch_ku<T>(KU_CHEB, a, modal_of<T>(c), s));
         std::swap(L.x, L.xt);
