@@ -145,6 +145,10 @@ double ke_modal(const double* ke, KeModal<double>* out) {
             for (int r = 0; r < 2; ++r) dz[q][r] = v3(q, r, 1) - v3(q, r, 0);
         }
         modal_element<double>(*out, 1.0, dxb, dxt, dyb, dyt, dz, f);
+        // the energy form on the unit vector gives the diagonal entry
+        V3<double> bm[8];
+        modal_amplitudes<double>(dxb, dxt, dyb, dyt, dz, bm);
+        dev = std::max(dev, std::fabs(modal_energy<double>(*out, bm) - ke[col * 24 + col]));
         for (int a = 0; a < 8; ++a) {
             const V3<double>& fa = f[LOCAL[a][0]][LOCAL[a][1]][LOCAL[a][2]];
             const double fc[3] = {fa.xy.x, fa.xy.y, fa.z};

@@ -170,6 +170,44 @@ __host__ __device__ __forceinline__ V3<T> v3zero() {
 //   dyb[px] = u(px,1,0) - u(px,0,0),  dyt[px] = u(px,1,1) - u(px,0,1)
 //   dz[px][py] = u(px,py,1) - u(px,py,0)
 // and writes the corner forces f[px][py][pz].
+// Mode amplitudes b1..b7 (x y z xy yz zx xyz) of a brick from its edge differences: the
+// Walsh-Hadamard transform of the corner values, taken through the edges.
+#pragma nv_exec_check_disable
+template <class T>
+__host__ __device__ __forceinline__ void modal_amplitudes(const V3<T> (&dxb)[2], const V3<T> (&dxt)[2],
+                                                          const V3<T> (&dyb)[2], const V3<T> (&dyt)[2],
+                                                          const V3<T> (&dz)[2][2], V3<T> (&b)[8]) {
+    const V3<T> s0 = dxb[0] + dxb[1], s1 = dxt[0] + dxt[1];
+    b[1] = s0 + s1;
+    b[6] = s1 - s0;
+    const V3<T> p0 = dxb[1] - dxb[0], p1 = dxt[1] - dxt[0];
+    b[4] = p0 + p1;
+    b[7] = p1 - p0;
+    const V3<T> t0 = dyb[0] + dyb[1], t1 = dyt[0] + dyt[1];
+    b[2] = t0 + t1;
+    b[5] = t1 - t0;
+    b[3] = (dz[0][0] + dz[1][0]) + (dz[0][1] + dz[1][1]);
+}
+
+// u_e^T Ke u_e (unit E) from the mode amplitudes: beta^T (KA / 64) beta written as sums of
+// squares in which every rigid rotation cancels inside a square (b1y + b2x for a rotation
+// about z, ...), so FP32 keeps the energy of an element that turns a lot but strains little.
+#pragma nv_exec_check_disable
+template <class T>
+__host__ __device__ __forceinline__ T modal_energy(const KeModal<T>& k, const V3<T> (&b)[8]) {
+    const T b1x = b[1].xy.x, b1y = b[1].xy.y, b1z = b[1].z, b2x = b[2].xy.x, b2y = b[2].xy.y, b2z = b[2].z;
+    const T b3x = b[3].xy.x, b3y = b[3].xy.y, b3z = b[3].z, b4x = b[4].xy.x, b4y = b[4].xy.y, b4z = b[4].z;
+    const T b5x = b[5].xy.x, b5y = b[5].xy.y, b5z = b[5].z, b6x = b[6].xy.x, b6y = b[6].xy.y, b6z = b[6].z;
+    const T tr = b1x + b2y + b3z, s3 = b4z + b5x + b6y;
+    const T q1 = b1y + b2x, q2 = b1z + b3x, q3 = b2z + b3y;
+    T e = k.ab * (b1x * b1x + b2y * b2y + b3z * b3z) + k.b * tr * tr + k.c * (q1 * q1 + q2 * q2 + q3 * q3);
+    e += k.d * (b4x * b4x + b5z * b5z + b4y * b4y + b6z * b6z + b5y * b5y + b6x * b6x);
+    e += T(2) * k.f * (b4x * b5z + b4y * b6z + b5y * b6x);
+    e += k.gh * (b4z * b4z + b5x * b5x + b6y * b6y) + k.h * s3 * s3;
+    e += k.j * (b[7].xy.x * b[7].xy.x + b[7].xy.y * b[7].xy.y + b[7].z * b[7].z);
+    return e;
+}
+
 #pragma nv_exec_check_disable
 template <class T>
 __host__ __device__ __forceinline__ void modal_element(const KeModal<T>& k, T E, const V3<T> (&dxb)[2],
@@ -177,13 +215,15 @@ __host__ __device__ __forceinline__ void modal_element(const KeModal<T>& k, T E,
                                                        const V3<T> (&dyt)[2], const V3<T> (&dz)[2][2],
                                                        V3<T> (&f)[2][2][2]) {
     // mode amplitudes (Walsh-Hadamard transform through the edges)
-    const V3<T> s0 = dxb[0] + dxb[1], s1 = dxt[0] + dxt[1];
-    const V3<T> b1 = s0 + s1, b6 = s1 - s0;
-    const V3<T> p0 = dxb[1] - dxb[0], p1 = dxt[1] - dxt[0];
-    const V3<T> b4 = p0 + p1, b7 = p1 - p0;
-    const V3<T> t0 = dyb[0] + dyb[1], t1 = dyt[0] + dyt[1];
-    const V3<T> b2 = t0 + t1, b5 = t1 - t0;
-    const V3<T> b3 = (dz[0][0] + dz[1][0]) + (dz[0][1] + dz[1][1]);
+    V3<T> bm[8];
+    modal_amplitudes<T>(dxb, dxt, dyb, dyt, dz, bm);
+    const V3<T>& b1 = bm[1];
+    const V3<T>& b2 = bm[2];
+    const V3<T>& b3 = bm[3];
+    const V3<T>& b4 = bm[4];
+    const V3<T>& b5 = bm[5];
+    const V3<T>& b6 = bm[6];
+    const V3<T>& b7 = bm[7];
     // the sparse modal stiffness, scaled by E
     const T ab = E * k.ab, bb = E * k.b, cc = E * k.c, dd = E * k.d, ff = E * k.f, gh = E * k.gh, hh = E * k.h,
             jj = E * k.j;

@@ -236,10 +236,6 @@ int stiffness_scale(anl_ctx* c, const float* xphys, const float* phi, double E0,
 
 // ------------------------------------------------------------------ sensitivity
 
-struct KeFull {
-    float k[24 * 24];
-};
-
 constexpr int kMaxCases = 16;
 struct SensArgs {
     Dims d;
@@ -257,33 +253,45 @@ struct SensArgs {
     int energy_only;
 };
 
-// u_e^T Ke u_e with u_e taken relative to the element's first node (Ke annihilates
-// translations), so FP32 products scale with the strain, not with |u|.
-__device__ __forceinline__ float element_energy(const KeFull& K, const double* u, const Dims& d, int i, int j, int k) {
-    const int64_t n0 = d.node(i, j, k);
+// u_e^T Ke u_e from the modal energy form (modal_energy): edge differences are formed in
+// FP64 and rounded to FP32, and rigid rotations cancel inside squares, so the result keeps its
+// accuracy relative to the element's own strain energy.
+__device__ __forceinline__ float element_energy(const KeModal<float>& K, const double* u, const Dims& d, int i, int j,
+                                                int k) {
     const int64_t sx = 1, sy = d.nx + 1, sz = (int64_t)(d.nx + 1) * (d.ny + 1);
-    const int64_t off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
-    const double b0 = u[3 * n0], b1 = u[3 * n0 + 1], b2 = u[3 * n0 + 2];
-    float dv[21];
+    const int64_t n0 = d.node(i, j, k);
+    double c[2][2][2][3];
 #pragma unroll
-    for (int a = 1; a < 8; ++a) {
-        const int64_t n = n0 + off[a];
-        dv[3 * (a - 1)] = (float)(u[3 * n] - b0);
-        dv[3 * (a - 1) + 1] = (float)(u[3 * n + 1] - b1);
-        dv[3 * (a - 1) + 2] = (float)(u[3 * n + 2] - b2);
+    for (int q = 0; q < 8; ++q) {
+        const int px = q & 1, py = (q >> 1) & 1, pz = (q >> 2) & 1;
+        const int64_t n = n0 + px * sx + py * sy + pz * sz;
+        c[px][py][pz][0] = u[3 * n];
+        c[px][py][pz][1] = u[3 * n + 1];
+        c[px][py][pz][2] = u[3 * n + 2];
     }
-    float ce = 0.f;
+    auto diff = [&](int ax, int bx, int ay, int by, int az, int bz) {
+        V3<float> v;
+        v.xy.x = (float)(c[ax][ay][az][0] - c[bx][by][bz][0]);
+        v.xy.y = (float)(c[ax][ay][az][1] - c[bx][by][bz][1]);
+        v.z = (float)(c[ax][ay][az][2] - c[bx][by][bz][2]);
+        return v;
+    };
+    V3<float> dxb[2], dxt[2], dyb[2], dyt[2], dz[2][2];
 #pragma unroll
-    for (int r = 0; r < 21; ++r) {
-        float t = 0.f;
+    for (int q = 0; q < 2; ++q) {
+        dxb[q] = diff(1, 0, q, q, 0, 0);
+        dxt[q] = diff(1, 0, q, q, 1, 1);
+        dyb[q] = diff(q, q, 1, 0, 0, 0);
+        dyt[q] = diff(q, q, 1, 0, 1, 1);
 #pragma unroll
-        for (int q = 0; q < 21; ++q) t = fmaf(K.k[(r + 3) * 24 + q + 3], dv[q], t);
-        ce = fmaf(dv[r], t, ce);
+        for (int r = 0; r < 2; ++r) dz[q][r] = diff(q, q, r, r, 1, 0);
     }
-    return ce;
+    V3<float> bm[8];
+    modal_amplitudes<float>(dxb, dxt, dyb, dyt, dz, bm);
+    return modal_energy<float>(K, bm);
 }
 
-__global__ void k_sens(SensArgs a, KeFull K) {
+__global__ void k_sens(SensArgs a, KeModal<float> K) {
     const Dims d = a.d;
     const int64_t ne = d.ne();
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
@@ -331,10 +339,8 @@ int sensitivity(anl_ctx* c, const double* u, int nrhs, const double* coef, const
     a.out = out;
     a.dv = energy_only ? nullptr : dv;
     a.energy_only = energy_only ? 1 : 0;
-    KeFull K;
-    for (int t = 0; t < 576; ++t) K.k[t] = (float)c->ke[t];
     const int64_t ne = c->d.ne();
-    k_sens<<<dgrid(ne), DT, 0, s>>>(a, K);
+    k_sens<<<dgrid(ne), DT, 0, s>>>(a, c->kmf);
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }

@@ -170,8 +170,10 @@ class FEM:
         self.log(f"  system: {self.act.size:,} elements, {self.nfree:,} free dofs, "
                  f"matrix-free on the GPU, built in {time.time() - t0:.1f} s")
 
-    def _ctx(self, fp64):
-        key = "fp64" if fp64 else "fp32"
+    def _ctx(self, fp64, lane=0):
+        """The solver context of a precision; lanes > 0 are extra contexts that solve other
+        load cases at the same time, each on its own stream."""
+        key = ("fp64" if fp64 else "fp32", lane)
         if key not in self._ctxs:
             c = Context(self.grid.shape, self.grid.h, self.nu, fp64=fp64)
             c.set_domain(self.active_t, self.fixed_t)
@@ -197,16 +199,89 @@ class FEM:
 
     def solve_device(self, escale, F, X, rtol=1e-8, maxiter=2000, rebuild=True):
         """Device-level solve: F, X (nrhs, 3*nnode) float64 CUDA tensors, X holds the
-        initial guesses and receives the solutions. Raises SolverError like fem.py:225-229."""
-        ctx = self._ctx(fp64=rtol < FP32_RTOL_FLOOR)
-        st, iters, relres = ctx.solve(escale, F, X, rtol, maxiter, rebuild)
+        initial guesses and receives the solutions. Raises SolverError like fem.py:225-229.
+
+        The reference solves its load cases one after the other (fem.py:217-231). Here the
+        cases are solved as a batch: a case whose load is a scalar multiple of another's
+        (for example the +x / -x pair of a load set) takes that multiple of its solution,
+        because the problem is linear; the remaining distinct cases run at the same time,
+        each in its own context and stream, so the latency-bound coarse levels of their
+        V-cycles overlap on the GPU."""
+        fp64 = rtol < FP32_RTOL_FLOOR
+        nrhs = F.shape[0] if F.dim() == 2 else 1
+        if nrhs == 1:
+            st, iters, relres = self._ctx(fp64).solve(escale, F, X, rtol, maxiter, rebuild)
+            sts = [st]
+        else:
+            groups = self._multiple_groups(F, fp64)
+            reps = [g[0] for g in groups]
+            res = self._solve_lanes(escale, F, X, reps, rtol, maxiter, rebuild, fp64)
+            iters, relres, sts = [0] * nrhs, [0.0] * nrhs, []
+            for (rep, members), (st, it, rr) in zip(groups, res):
+                sts.append(st)
+                iters[rep], relres[rep] = it, rr
+                for m, scale in members:
+                    X[m].copy_(X[rep]).mul_(scale)
+                    iters[m], relres[m] = it, rr
         if rebuild:
             self.amg_builds += 1
-        if st != N.ANL_OK:
+        if any(st != N.ANL_OK for st in sts):
             raise SolverError(SOLVER_MESSAGE.format(maxiter=maxiter))
         self.cg_iters.extend(iters)
         self.relres.extend(relres)
         return iters
+
+    def _multiple_groups(self, F, fp64):
+        """[(representative, [(case, scale), ...]), ...]: cases whose load is a scalar
+        multiple of an earlier case's (collinear to 1e-12 in FP64) join that case."""
+        ctx = self._ctx(fp64)
+        n = F.shape[0]
+        norm2 = [ctx.dot(F[i], F[i]) for i in range(n)]
+        groups = []
+        for i in range(n):
+            placed = False
+            for g in groups:
+                r = g[0]
+                if norm2[r] == 0.0 or norm2[i] == 0.0:
+                    continue
+                d = ctx.dot(F[r], F[i])
+                if d * d >= (1.0 - 1e-12) * norm2[r] * norm2[i]:
+                    g[1].append((i, d / norm2[r]))
+                    placed = True
+                    break
+            if not placed:
+                groups.append((i, []))
+        return groups
+
+    def _solve_lanes(self, escale, F, X, reps, rtol, maxiter, rebuild, fp64):
+        """Solves F[reps[k]] in context lane k on stream k, concurrently (host threads; the
+        library releases the GIL in every call). Returns [(status, iters, relres)]."""
+        import concurrent.futures as cf
+        main = torch.cuda.current_stream()
+        dev = torch.cuda.current_device()
+        ctxs = [self._ctx(fp64, lane=k) for k in range(len(reps))]
+        if not hasattr(self, "_streams"):
+            self._streams = []
+        while len(self._streams) < len(reps):
+            self._streams.append(torch.cuda.Stream(device=dev))
+        streams = self._streams[:len(reps)]
+        for st in streams:
+            st.wait_stream(main)
+
+        def work(k):
+            torch.cuda.set_device(dev)
+            with torch.cuda.stream(streams[k]):
+                r = reps[k]
+                st, it, rr = ctxs[k].solve(escale, F[r:r + 1], X[r:r + 1], rtol, maxiter, rebuild)
+                return st, it[0], rr[0]
+        if len(reps) == 1:
+            out = [work(0)]
+        else:
+            with cf.ThreadPoolExecutor(max_workers=len(reps)) as ex:
+                out = list(ex.map(work, range(len(reps))))
+        for st in streams:
+            main.wait_stream(st)
+        return out
 
     def solve(self, K, F_list, x0_list=None, rebuild=True, rtol=1e-8, maxiter=2000):
         """fem.py:206-232: reduced loads in, reduced displacements out."""

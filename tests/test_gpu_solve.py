@@ -141,3 +141,44 @@ def test_log_line_format_matches_reference(golden):
     its = [l for l in lines if l.startswith("  it ")]
     assert len(its) == 3 and all(pat.match(l) for l in its)
     assert all(pat.match(l) for l in ref if l.startswith("  it "))
+
+
+def test_six_load_cases_batched_match_one_by_one():
+    """The batched multi-case solve (scalar-multiple cases folded, the rest solved at the
+    same time on separate streams) against one solve per case."""
+    import torch
+    w = P.six_case_bracket(scale=1.0 / 6.0)
+    grid = _grid(w.shape)
+    fem = G.FEM(grid, w.active, w.fixed, 0.3)
+    rng = np.random.default_rng(3)
+    E = np.exp(rng.normal(0.0, 1.0, w.nelem)) * w.active
+    escale = torch.as_tensor(E, dtype=torch.float32, device="cuda")
+    mask = fem._mask_t.double()
+    F = torch.stack([torch.as_tensor(w.loads[k], device="cuda") * mask for k in w.loads])
+    X = torch.zeros_like(F)
+    fem.solve_device(escale, F, X, rtol=1e-10)
+    for i in range(F.shape[0]):
+        Xi = torch.zeros_like(F[i:i + 1])
+        fem.solve_device(escale, F[i:i + 1].clone(), Xi, rtol=1e-10)
+        assert float((X[i] - Xi[0]).abs().max()) <= 1e-7 * float(Xi.abs().max())
+    # the -x case is the +x solution negated, exactly
+    assert torch.equal(X[1], -X[0])
+    fem.close()
+
+
+def test_six_case_simp_matches_oracle(oracle):
+    w = P.six_case_bracket(scale=1.0 / 6.0)
+    kw = dict(iters=4, r_mm=1.5, p_final=3.0, move=0.2, tol=0.0, x0=np.full(w.nelem, 0.25), beta_max=0.0,
+              log=lambda *a: None, rtol=1e-8)
+    old = O.EMIN
+    O.EMIN = 1e-9
+    try:
+        got = O.simp(_grid(w.shape), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, 1.0, 0.3, 0.25, **kw)
+    finally:
+        O.EMIN = old
+    want = oracle.simp(w.shape, 1.0, w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, 1.0, 0.3, 0.25,
+                       emin=1e-9, **kw)
+    cg = np.array([h["compliance"] for h in got["history"]])
+    co = np.array([h["compliance"] for h in want["history"]])
+    assert np.abs(cg / co - 1).max() < 1e-5
+    assert np.abs(got["x"] - want["x"]).max() < 1e-3
