@@ -30,7 +30,7 @@ enum {
     ANL_ERR_BREAKDOWN = 3, /* p.Kp <= 0: the operator is not positive definite */
     ANL_ERR_BADARG = 4,
     ANL_ERR_CUDA = 5,
-    ANL_ERR_SINGULAR = 6, /* coarse-grid factorisation failed */
+    ANL_ERR_SINGULAR = 6, /* reserved (tiny coarse-grid pivots are regularised, not reported) */
     ANL_ERR_NOMEM = 7,
     ANL_ERR_STATE = 8 /* a call that needs anl_set_domain / anl_filter_init came first */
 };

@@ -182,3 +182,16 @@ def test_six_case_simp_matches_oracle(oracle):
     co = np.array([h["compliance"] for h in want["history"]])
     assert np.abs(cg / co - 1).max() < 1e-5
     assert np.abs(got["x"] - want["x"]).max() < 1e-3
+
+
+def test_many_parts_in_lanes_match_one_by_one():
+    """Independent parts run as concurrent lanes give exactly the results of running them one
+    after another (the kernels are deterministic; lanes only overlap them)."""
+    from anneal_gb300 import batch as B
+    parts = B.seeded_parts(4, seed=5)
+    parts = [P.cantilever(min(w.shape[0], 40), min(w.shape[1], 20), min(w.shape[2], 20), vf=w.vf, r_vox=w.r_vox,
+                          emin=1e-9) for w in parts]
+    _, seq = B.run_parts(parts, 3, 1)
+    _, par = B.run_parts(parts, 3, 3)
+    for a, b in zip(seq, par):
+        assert a["compliance"] == b["compliance"] and a["shape"] == b["shape"]
