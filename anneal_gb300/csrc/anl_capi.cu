@@ -19,6 +19,11 @@ static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+std::recursive_mutex& device_sync_mutex() {
+    static std::recursive_mutex m;
+    return m;
+}
+
 void set_error(const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -201,6 +206,7 @@ static cudaError_t upload_cheb(anl_ctx* c) {
 
 static void free_ctx(anl_ctx* c) {
     if (!c) return;
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     auto f = [](void* p) {
         if (p) cudaFree(p);
     };
@@ -421,6 +427,7 @@ int64_t anl_launch_count(void) { return (int64_t)anl::g_launches.load(); }
 
 int anl_ctx_create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, int flags) {
     anl::g_err[0] = 0;
+    std::lock_guard<std::recursive_mutex> lock(anl::device_sync_mutex());
     return create(out, nx, ny, nz, h, nu, flags);
 }
 

@@ -11,6 +11,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "../../include/anneal_gb300.h"
 
@@ -46,6 +47,12 @@ namespace anl {
     } while (0)
 
 void set_error(const char* fmt, ...);
+
+// Held while a stream is captured into a CUDA graph and around every call that synchronises
+// the whole device (cudaFree, cudaFreeHost, context set-up): such a call from another host
+// thread would invalidate an ongoing capture, and several contexts may run in parallel
+// threads (one per load case or per part).
+std::recursive_mutex& device_sync_mutex();
 void count_launch();
 void count_launches(long long n);  // kernels replayed by a CUDA graph
 

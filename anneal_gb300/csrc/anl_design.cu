@@ -174,6 +174,7 @@ int filter_init(anl_ctx* c, double r, cudaStream_t s) {
                 const double v = r - std::sqrt((double)(dx * dx + dy * dy + dz * dz));
                 w[(dx + R) + W * ((dy + R) + W * (dz + R))] = v > 0 ? (float)v : 0.f;
             }
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     if (c->filt.w) cudaFree(c->filt.w);
     c->filt.w = nullptr;
     ANL_CUDA(cudaMalloc(&c->filt.w, sizeof(float) * w.size()));

@@ -546,6 +546,7 @@ struct anl_mc {
 namespace {
 
 void mc_free(anl_mc* m) {
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     cudaFree(m->g);
     cudaFree(m->code);
     cudaFree(m->cnt);
@@ -571,6 +572,7 @@ void mc_free(anl_mc* m) {
 template <class P>
 int grow(P*& p, size_t& cap, size_t need, size_t elem) {
     if (need <= cap) return ANL_OK;
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     cudaFree(p);
     p = nullptr;
     cap = 0;

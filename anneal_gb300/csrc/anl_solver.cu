@@ -761,6 +761,7 @@ static int capture_chunk(anl_ctx* c, int chunk) {
         c->cg_exec = nullptr;
     }
     cudaGraph_t g = nullptr;
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     ANL_CUDA(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
     const int st = enqueue_chunk<T>(c, chunk, c->cap_stream);
     const cudaError_t e = cudaStreamEndCapture(c->cap_stream, &g);
