@@ -273,7 +273,10 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         return ANL_ERR_BADARG;
     }
     for (int a = 0; a < 8; ++a)
-        for (int t = 0; t < 9; ++t) c->kbf.blk[a][t] = (float)c->kbd.blk[a][t];
+        for (int t = 0; t < 9; ++t) {
+            c->kbf.blk[a][t] = (float)c->kbd.blk[a][t];
+            c->kbf_lo.blk[a][t] = (float)(c->kbd.blk[a][t] - (double)c->kbf.blk[a][t]);
+        }
     const double mdev = ke_modal(c->ke, &c->kmd);
     if (!(mdev < 1e-12)) {
         set_error("element matrix lacks the isotropic mode structure (deviation %g)", mdev);

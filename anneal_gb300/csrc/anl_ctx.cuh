@@ -49,6 +49,7 @@ struct anl_ctx {
     double* ke_d = nullptr;         // Ke(1) on the device (coarse assembly)
     anl::KeBlocks<double> kbd{};
     anl::KeBlocks<float> kbf{};
+    anl::KeBlocks<float> kbf_lo{};  // kbd - kbf: with kbf, the FP64 blocks as float pairs
     anl::KeModal<double> kmd{};
     anl::KeModal<float> kmf{};
     double kdiag = 0.0;

@@ -49,6 +49,7 @@ struct ResidHpArgs {
     int partial_capacity = 0;
     double* rr_out = nullptr;
 };
-int launch_resid_hp(const ResidHpArgs& a, const KeBlocks<float>& kb, cudaStream_t s);
+// kb + kbl: the FP64 element blocks as float pairs (hi, lo)
+int launch_resid_hp(const ResidHpArgs& a, const KeBlocks<float>& kb, const KeBlocks<float>& kbl, cudaStream_t s);
 
 }  // namespace anl

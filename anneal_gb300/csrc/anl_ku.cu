@@ -471,12 +471,14 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
 
 // ------------------------------------------------------------------ accurate residual
 //
-// r = b - K32 x for x held in FP64 (as the pair x_hi + x_lo of floats), where K32 is the
-// FP32 operator above (the element blocks rounded to FP32). Differences, products and sums
-// are carried as unevaluated float pairs (TwoSum / TwoProd), so the result is accurate to
-// about eps^2 of the summed terms: the FP32 CG can certify ||b - K32 x|| <= rtol ||b||
-// far below the FP32 rounding floor of a plain evaluation (eps |K| |x|), at a fraction of
-// the cost of FP64 arithmetic on this part.
+// r = b - K x for x held in FP64 (as the pair x_hi + x_lo of floats), with K the operator of
+// the FP64 element blocks (each block entry a float pair hi + lo) and the FP32 element scales.
+// Differences, products and sums are carried as unevaluated float pairs (TwoSum / TwoProd),
+// so the result is accurate to about eps^2 of the summed terms: the FP32 CG certifies
+// ||b - K x|| <= rtol ||b|| for the FP64 operator, far below the FP32 rounding floor of a
+// plain evaluation (eps |K| |x|), at a fraction of the cost of FP64 arithmetic on this part.
+// The FP32 modal operator drives the recurrence; the periodic replacements by this residual
+// make the iteration converge to the FP64 operator's solution (iterative refinement).
 
 struct F2 {
     float s, c;
@@ -489,7 +491,8 @@ __device__ __forceinline__ void f2_add(F2& a, float p) {
     a.c += e;
 }
 
-__global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, KeBlocks<float> kb) {
+__global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, KeBlocks<float> kb,
+                                                                KeBlocks<float> kbl) {
     __shared__ float sh[3][KU_HY][KU_HX][3];
     __shared__ float sl[3][KU_HY][KU_HX][3];
     __shared__ float sE[2][KU_EY][KU_EX];
@@ -569,6 +572,7 @@ __global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, Ke
                         tc[c] = sg * (de + dl);
                     }
                     const float* B = kb.blk[dlt];
+                    const float* Bl = kbl.blk[dlt];  // the FP64 blocks = B + Bl to ~eps^2
 #pragma unroll
                     for (int rr3 = 0; rr3 < 3; ++rr3)
 #pragma unroll
@@ -576,7 +580,7 @@ __global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, Ke
                             float p, e;
                             two_prod(B[3 * rr3 + c], th[c], p, e);
                             f2_add(w[rr3], p);
-                            w[rr3].c += e + B[3 * rr3 + c] * tc[c];
+                            w[rr3].c += e + B[3 * rr3 + c] * tc[c] + Bl[3 * rr3 + c] * th[c];
                         }
                 }
 #pragma unroll
@@ -610,7 +614,7 @@ __global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, Ke
     }
 }
 
-int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, cudaStream_t s) {
+int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, const KeBlocks<float>& kbl, cudaStream_t s) {
     ResidHpArgs a = args;
     const Dims& d = a.d;
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
@@ -622,7 +626,7 @@ int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, cudaStre
                   a.partial_capacity);
         return ANL_ERR_BADARG;
     }
-    ku_resid_hp_kernel<<<grid, dim3(KU_BX, KU_BY), 0, s>>>(a, kb);
+    ku_resid_hp_kernel<<<grid, dim3(KU_BX, KU_BY), 0, s>>>(a, kb, kbl);
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }

@@ -720,7 +720,7 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s, bool accurat
     a.counter = c->counter;
     a.partial_capacity = c->part_cap;
     a.rr_out = c->red_out + 8;
-    ANL_TRY(launch_resid_hp(a, c->kbf, s));
+    ANL_TRY(launch_resid_hp(a, c->kbf, c->kbf_lo, s));
     k_resid_state<<<1, 1, 0, s>>>(c->sc, c->red_out + 8, set_state);
     ANL_LAUNCH_CHECK();
     return ANL_OK;
