@@ -32,7 +32,7 @@ EXPORTS = [
     "anl_launch_count", "anl_mg_info", "anl_dot_static",
     "anl_mc_create", "anl_mc_destroy", "anl_mc_extract", "anl_mc_smooth", "anl_mc_components", "anl_mc_copy",
     "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
-    "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam",
+    "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam", "anl_element_stress",
 ]
 
 
@@ -89,6 +89,7 @@ _SIGS = {
     "anl_nn_up2": (I, [P, P, I, I, I, I, I, P]),
     "anl_nn_mse": (I, [P, P, P, P, I, I64, P, P, P, P]),
     "anl_nn_adam": (I, [P, P, P, P, I64, D, D, D, D, I, P]),
+    "anl_element_stress": (I, [P, P, P, D, P, P, P]),
 }
 
 

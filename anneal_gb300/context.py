@@ -144,6 +144,17 @@ class Context:
         _chk(ce, _F32, self.ne, "ce")
         N.check(self.lib.anl_element_energy(self._h, _p(u), _p(ce), _stream()), "anl_element_energy")
 
+    def element_stress(self, u, E_material, sig=None, vm=None):
+        """E_material: float64 CUDA tensor (ne) or a number; sig (ne, 6) / vm (ne) float64."""
+        _chk(u, _F64, self.ndof, "u")
+        if torch.is_tensor(E_material):
+            _chk(E_material, _F64, self.ne, "E_material")
+            em, es = _p(E_material), 0.0
+        else:
+            em, es = None, float(E_material)
+        N.check(self.lib.anl_element_stress(self._h, _p(u), em, es, _p(sig) if sig is not None else None,
+                                            _p(vm) if vm is not None else None, _stream()), "anl_element_stress")
+
     def sensitivity(self, U, coef, xphys, dxp, phi, p, emin, E0, out, dv=None):
         nrhs = len(coef)
         _chk(U, _F64, nrhs * self.ndof, "U")

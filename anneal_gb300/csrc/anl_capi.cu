@@ -173,6 +173,8 @@ int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, in
                  int rebuild, int* iters, double* relres, cudaStream_t s);
 int solver_dot(anl_ctx* c, const double* a, const double* b, double* out, cudaStream_t s);
 int filter_init(anl_ctx* c, double r, cudaStream_t s);
+int element_stress(anl_ctx* c, const double* u, const double* Emat, double Escalar, double* sig, double* vm,
+                   cudaStream_t s);
 int filter_apply(anl_ctx* c, bool forward, const float* in, float* out, cudaStream_t s);
 int physical(anl_ctx* c, const float* x, const uint8_t* frozen, double beta, double eta, float* xphys, float* dxp,
              cudaStream_t s);
@@ -477,6 +479,16 @@ int anl_element_energy(anl_ctx* ctx, const double* u, float* ce, anl_stream_t st
         return ANL_ERR_STATE;
     }
     return sensitivity(ctx, u, 1, nullptr, nullptr, nullptr, nullptr, 1.0, 0.0, 1.0, ce, nullptr, true, S(stream));
+}
+
+int anl_element_stress(anl_ctx* ctx, const double* u, const double* E_material, double E_scalar, double* sig,
+                       double* vm, anl_stream_t stream) {
+    NEED(ctx && u && (sig || vm), "anl_element_stress: null argument");
+    if (!ctx->domain_set) {
+        set_error("anl_element_stress: call anl_set_domain first");
+        return ANL_ERR_STATE;
+    }
+    return element_stress(ctx, u, E_material, E_scalar, sig, vm, S(stream));
 }
 
 int anl_sensitivity(anl_ctx* ctx, const double* u, int nrhs, const double* coef, const float* xphys, const float* dxp,

@@ -316,6 +316,59 @@ __global__ void k_sens(SensArgs a, KeModal<float> K) {
     }
 }
 
+// Element-centre stress (fem.py:244-263): at the centre only the linear modes have slopes,
+// du_c/dx_d = b_dc / (4 h) with b_dc = sum of the 4 edge differences of component c along d,
+// so the strain is eps = (b1x, b2y, b3z, b2x + b1y, b3y + b2z, b1z + b3x) / (4 h) (Voigt,
+// engineering shear) and sigma = E D eps with the isotropic D of unit modulus. FP64.
+__global__ void k_stress(Dims d, const uint8_t* active, const double* u, const double* Emat, double Escalar, double h,
+                         double lam, double mu, double* sig, double* vm) {
+    const int64_t ne = d.ne();
+    const int64_t sx = 1, sy = d.nx + 1, sz = (int64_t)(d.nx + 1) * (d.ny + 1);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        if (!active[e]) {
+            if (sig)
+                for (int q = 0; q < 6; ++q) sig[6 * e + q] = 0.0;
+            if (vm) vm[e] = 0.0;
+            continue;
+        }
+        const int i = (int)(e % d.nx), j = (int)((e / d.nx) % d.ny), k = (int)(e / ((int64_t)d.nx * d.ny));
+        const int64_t n0 = d.node(i, j, k);
+        double g[3][3] = {};  // g[c][dir]: sum of edge differences of component c along dir
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int a = q & 1, b = q >> 1;
+            const int64_t ex = n0 + a * sy + b * sz, ey = n0 + a * sx + b * sz, ez = n0 + a * sx + b * sy;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                g[c][0] += u[3 * (ex + sx) + c] - u[3 * ex + c];
+                g[c][1] += u[3 * (ey + sy) + c] - u[3 * ey + c];
+                g[c][2] += u[3 * (ez + sz) + c] - u[3 * ez + c];
+            }
+        }
+        const double s = 1.0 / (4.0 * h);
+        const double exx = g[0][0] * s, eyy = g[1][1] * s, ezz = g[2][2] * s;
+        const double gxy = (g[0][1] + g[1][0]) * s, gyz = (g[1][2] + g[2][1]) * s, gzx = (g[2][0] + g[0][2]) * s;
+        const double E = Emat ? Emat[e] : Escalar;
+        const double tr = exx + eyy + ezz;
+        const double S[6] = {E * (lam * tr + 2 * mu * exx), E * (lam * tr + 2 * mu * eyy), E * (lam * tr + 2 * mu * ezz),
+                             E * mu * gxy, E * mu * gyz, E * mu * gzx};
+        if (sig)
+            for (int q = 0; q < 6; ++q) sig[6 * e + q] = S[q];
+        if (vm)
+            vm[e] = sqrt(0.5 * ((S[0] - S[1]) * (S[0] - S[1]) + (S[1] - S[2]) * (S[1] - S[2]) + (S[2] - S[0]) * (S[2] - S[0])) +
+                         3.0 * (S[3] * S[3] + S[4] * S[4] + S[5] * S[5]));
+    }
+}
+
+int element_stress(anl_ctx* c, const double* u, const double* Emat, double Escalar, double* sig, double* vm,
+                   cudaStream_t s) {
+    const double nu = c->nu;
+    const double lam = nu / ((1 + nu) * (1 - 2 * nu)), mu = 1.0 / (2 * (1 + nu));
+    k_stress<<<dgrid(c->d.ne()), DT, 0, s>>>(c->d, c->active, u, Emat, Escalar, c->h, lam, mu, sig, vm);
+    ANL_LAUNCH_CHECK();
+    return ANL_OK;
+}
+
 int sensitivity(anl_ctx* c, const double* u, int nrhs, const double* coef, const float* xphys, const float* dxp,
                 const float* phi, double p, double emin, double E0, float* out, float* dv, bool energy_only,
                 cudaStream_t s) {

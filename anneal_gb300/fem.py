@@ -305,6 +305,42 @@ class FEM:
         ctx.element_energy(to_dev(u_full, torch.float64), ce)
         return ce.cpu().numpy().astype(float)[self.act]
 
+    def _stress_device(self, u_full, E_material, want_sig, want_vm):
+        ctx = self._ctx(fp64=False)
+        u = to_dev(np.asarray(u_full, float), torch.float64)
+        ne = self.grid.nelem
+        if np.ndim(E_material):
+            Ef = np.zeros(ne)
+            Ef[self.act] = np.asarray(E_material, float)
+            E = to_dev(Ef, torch.float64)
+        else:
+            E = float(E_material)
+        sig = torch.empty((ne, 6), dtype=torch.float64, device="cuda") if want_sig else None
+        vm = torch.empty(ne, dtype=torch.float64, device="cuda") if want_vm else None
+        ctx.element_stress(u, E, sig, vm)
+        return sig, vm
+
+    def stress(self, u_full, E_material):
+        """Element-centre stress, Voigt order xx yy zz xy yz zx, shape (n_active, 6)
+        (fem.py:244-250), computed on the GPU."""
+        sig, _ = self._stress_device(u_full, E_material, True, False)
+        return sig.cpu().numpy()[self.act]
+
+    @staticmethod
+    def normal_stress(sig, d):
+        """Normal stress on planes across direction d, d^T sigma d (fem.py:252-257)."""
+        d = np.asarray(d, float)
+        d = d / np.linalg.norm(d)
+        S = np.asarray(sig)
+        T = np.stack([np.stack([S[:, 0], S[:, 3], S[:, 5]], -1), np.stack([S[:, 3], S[:, 1], S[:, 4]], -1),
+                      np.stack([S[:, 5], S[:, 4], S[:, 2]], -1)], -2)
+        return np.einsum("i,nij,j->n", d, T, d)
+
+    def von_mises(self, u_full, E_material):
+        """Element-centre von Mises stress (fem.py:259-263), computed on the GPU."""
+        _, vm = self._stress_device(u_full, E_material, False, True)
+        return vm.cpu().numpy()[self.act]
+
     def close(self):
         for c in self._ctxs.values():
             c.close()

@@ -185,6 +185,20 @@ def run_reference(args):
     return 0
 
 
+def replica_rate(local_ms, steps, world, device):
+    """Whole-job rate of `world` independent replicas that each ran `steps` steps in
+    local_ms: the slowest rank's time (max over ranks) bounds the job. Returns (rate in
+    steps/s, max ms)."""
+    t = float(local_ms)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t], device=device, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return world * steps / (t / 1e3), t
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -232,12 +246,7 @@ def run_gpu(args):
     barrier()
     launches = lib.anl_launch_count() - launches0
     cg_counts = run.fem.cg_iters[cg0:]
-    t_max = total_ms
-    if world > 1:
-        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = world * args.steps / (t_max / 1e3)
+    value, t_max = replica_rate(total_ms, args.steps, world, "cuda")
 
     # end to end: the design goes host -> device -> host around every step (pinned buffers)
     x_in = torch.empty(w.nelem, dtype=torch.float32).pin_memory()
@@ -256,11 +265,7 @@ def run_gpu(args):
         e2e_ms += e0.elapsed_time(e1)
         x_in.copy_(x_out)
     barrier()
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    e2e = world * args.steps / (e2e_ms / 1e3)
+    e2e, e2e_ms = replica_rate(e2e_ms, args.steps, world, "cuda")
 
     # dominant kernel: the fine-level K u, timed alone with CUDA events on this stream
     ctx = run.ctx

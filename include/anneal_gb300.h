@@ -148,6 +148,13 @@ int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const f
    nothing, frees nothing. */
 int anl_dot_static(const double* a, const double* b, int64_t n, double* out, anl_stream_t stream);
 
+/* Replaces FEM.stress / FEM.von_mises (fem.py:244-263): element-centre stress sigma = E D B0 u_e
+   (Voigt xx yy zz xy yz zx, engineering shear) and its von Mises value, FP64, on the full
+   element grid (zeros on inactive elements). E_material: per element (double, full grid) or
+   NULL to use E_scalar. sig (6 per element) or vm (1 per element) may be NULL. */
+int anl_element_stress(anl_ctx* ctx, const double* u, const double* E_material, double E_scalar, double* sig,
+                       double* vm, anl_stream_t stream);
+
 /* ---------------------------------------------------------------- iso-surface export */
 
 /* An export workspace: device buffers that grow to the largest field seen, the derived

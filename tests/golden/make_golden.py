@@ -241,6 +241,31 @@ def gen_validate(validate):
         json.dump(out, fh, indent=1)
 
 
+def gen_stress(fem):
+    """FEM.stress / von_mises / normal_stress (fem.py:244-263) on a cantilever solution, with
+    a per-element modulus (h = 0.5) and a scalar one."""
+    rng = np.random.default_rng(11)
+    g = fem.Grid((9, 4, 5), 0.5, (1.0, -2.0, 0.5))
+    active = rng.random(g.nelem) > 0.1
+    n = np.arange(g.nnode)
+    p = g.node_coords(n)
+    clamp = n[p[:, 0] < 1.0 + 1e-9]
+    fixed = (3 * clamp[:, None] + np.arange(3)).ravel()
+    model = fem.FEM(g, active, fixed, 0.3)
+    act = np.flatnonzero(active)
+    Ee = np.exp(rng.normal(0.0, 0.5, act.size))
+    F = np.zeros(3 * g.nnode)
+    tip = n[(abs(p[:, 0] - (1.0 + 9 * 0.5)) < 1e-9)]
+    F[3 * tip + 2] = -1.0 / tip.size
+    F[3 * tip] = 0.3 / tip.size
+    u = model.expand(model.solve(model.assemble(Ee), [model.reduce_load(F)], rtol=1e-12, maxiter=20000)[0])
+    Emat = np.exp(rng.normal(0.0, 0.3, act.size)) * 2000.0
+    sig = model.stress(u, Emat)
+    np.savez_compressed(os.path.join(HERE, "stress.npz"), shape=np.array(g.shape), h=g.h, origin=g.origin,
+                        active=active, fixed=fixed, u=u, Emat=Emat, sig=sig, vm=model.von_mises(u, Emat),
+                        vm_scalar=model.von_mises(u, 1500.0), sn=model.normal_stress(sig, (0.2, -0.3, 1.0)))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -253,7 +278,7 @@ def main():
             "simp_small": lambda: gen_simp_small(fem, optimize),
             "simp_small_tight": lambda: gen_simp_small(fem, optimize, rtol=1e-10),
             "simp_worst": lambda: gen_simp_worst(fem, optimize),
-            "validate": lambda: gen_validate(validate)}
+            "validate": lambda: gen_validate(validate), "stress": lambda: gen_stress(fem)}
     if not a.skip_config1:
         jobs["config1"] = lambda: gen_config1(fem, optimize)
     for name, fn in jobs.items():

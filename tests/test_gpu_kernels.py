@@ -175,3 +175,21 @@ def test_sensitivity_matches_oracle(oracle):
     got = out.cpu().numpy()[act]
     assert np.abs(got - want).max() <= 2e-6 * np.abs(want).max()
     assert np.abs(dv.cpu().numpy()[act] - phi[act] * dxp[act]).max() < 1e-6
+
+
+def test_stress_and_von_mises_match_reference(golden):
+    """FEM.stress / von_mises / normal_stress against the reference's own values
+    (fem.py:244-263) on a cantilever solution, per-element and scalar modulus."""
+    from anneal_gb300 import fem as G
+    g = golden("stress.npz")
+    grid = G.Grid(tuple(int(s) for s in g["shape"]), float(g["h"]), g["origin"])
+    fem = G.FEM(grid, g["active"], g["fixed"], 0.3)
+    sig = fem.stress(g["u"], g["Emat"])
+    assert np.abs(sig - g["sig"]).max() <= 1e-10 * np.abs(g["sig"]).max()
+    vm = fem.von_mises(g["u"], g["Emat"])
+    assert np.abs(vm - g["vm"]).max() <= 1e-10 * np.abs(g["vm"]).max()
+    vs = fem.von_mises(g["u"], 1500.0)
+    assert np.abs(vs - g["vm_scalar"]).max() <= 1e-10 * np.abs(g["vm_scalar"]).max()
+    sn = fem.normal_stress(sig, (0.2, -0.3, 1.0))
+    assert np.abs(sn - g["sn"]).max() <= 1e-10 * np.abs(g["sn"]).max()
+    fem.close()
