@@ -15,7 +15,7 @@ struct Level {
     float* E = nullptr;       // element scale (times h at level 0; children sum / 4 below)
     uint8_t* eact = nullptr;  // element is (or covers) an active element
     uint8_t* nmask = nullptr; // node mask bits
-    float* diag = nullptr;    // diagonal of K per node (the same for the 3 DOFs of a node)
+    float* diag = nullptr;    // inverse diagonal of K per node (the same for its 3 DOFs; 0 if unused)
     void* x = nullptr;        // V-cycle iterate (level 0: z = M r)
     void* xt = nullptr;       // Chebyshev double buffer
     void* b = nullptr;        // right-hand side (level 0: the CG residual r)

@@ -7,7 +7,9 @@ namespace anl {
 
 // ------------------------------------------------------------------ K u family
 
-enum { KU_APPLY = 0, KU_APPLY_DOT = 1, KU_RESID = 2, KU_CHEB = 3 };
+// KU_CHEB0: the first two Chebyshev steps from x = 0 in one pass: x1 = c2_0 D^-1 b is formed
+// on the fly from the staged b and diagonal, then x2 = x1 + c1_1 x1 + c2_1 D^-1 (b - K x1)
+enum { KU_APPLY = 0, KU_APPLY_DOT = 1, KU_RESID = 2, KU_CHEB = 3, KU_CHEB0 = 4 };
 
 template <class T>
 struct KuArgs {
@@ -23,6 +25,8 @@ struct KuArgs {
     T c1 = T(0), c2 = T(0);          // CHEB: d <- c1 d + c2 D^-1 (b - K u)
     const double* cheb = nullptr;    // CHEB: {c1, c2} in device memory (overrides c1, c2)
     int c1_zero = 0;                 // CHEB: first step of a sweep (c1 = 0, d is not read)
+    const double* cheb0 = nullptr;   // CHEB0: {c1_0, c2_0} of the step from x = 0
+    const float* diag = nullptr;     // CHEB0: inverse diagonal of K per node (0 where unused)
     T kdiag = T(0);                  // diagonal entry of Ke(1) (all 24 are equal)
     double* partials = nullptr;      // APPLY_DOT reduction scratch
     unsigned* counter = nullptr;

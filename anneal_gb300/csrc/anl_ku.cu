@@ -120,9 +120,11 @@ __device__ __forceinline__ void cp_async_wait() {
 template <class T, int MODE>
 struct KuSmem {
     static constexpr int NW = KmCfg<T>::NW;
-    static constexpr int NV = MODE == KU_CHEB ? 7 : 6;  // values passed to the next warp (+ E sum)
-    T u[KU_RING][NW + 1][32][3];
+    static constexpr bool CH = MODE == KU_CHEB || MODE == KU_CHEB0;
+    static constexpr int NV = CH ? 7 : 6;  // values passed to the next warp (+ E sum)
+    T u[KU_RING][NW + 1][32][3];           // staged node values (b in CHEB0)
     float E[KU_RING][NW][32];
+    float D[MODE == KU_CHEB0 ? KU_RING : 1][NW + 1][32];  // CHEB0: staged inverse diagonal
     T x[2][NW + 1][NV][32];
 };
 static_assert((KU_RING & (KU_RING - 1)) == 0, "the cp.async ring length must be a power of two");
@@ -140,6 +142,10 @@ struct KuTile {
     int NXn, NYn, NZn;
     int64_t plane, eplane;
     uint32_t s_u, s_uN, s_E;  // shared addresses of this thread's ring entries in slot 0
+    uint32_t s_D, s_DN;       // CHEB0: the inverse diagonal's ring entries
+    const T* src_base;        // staged node field: u, or b in CHEB0
+    T c2_0 = T(0);            // CHEB0: x1 = c2_0 D^-1 b
+    const float* iD = nullptr;
     // segment geometry
     bool r0in, rNin, ein, owner;
     int64_t n0, e0;
@@ -159,6 +165,10 @@ struct KuTile {
         s_u = (uint32_t)__cvta_generic_to_shared(&sm.u[0][w][lane][0]);
         s_uN = (uint32_t)__cvta_generic_to_shared(&sm.u[0][NW][lane][0]);
         s_E = (uint32_t)__cvta_generic_to_shared(&sm.E[0][w][lane]);
+        s_D = (uint32_t)__cvta_generic_to_shared(&sm.D[0][w][lane]);
+        s_DN = (uint32_t)__cvta_generic_to_shared(&sm.D[0][NW][lane]);
+        src_base = MODE == KU_CHEB0 ? a.b : a.u;
+        if (MODE == KU_CHEB0) c2_0 = T(a.cheb0[1]);
     }
 
     __device__ void set_column(int bx, int by, int k0) {
@@ -171,8 +181,9 @@ struct KuTile {
         n0 = (int64_t)ie + (int64_t)NXn * je;
         e0 = (int64_t)ie + (int64_t)a.d.nx * je;
         ik = k0 - 2;
-        iu = a.u + 3 * (n0 + (int64_t)(ik + 1) * plane);
+        iu = src_base + 3 * (n0 + (int64_t)(ik + 1) * plane);
         iE = a.E + e0 + (int64_t)ik * eplane;
+        if (MODE == KU_CHEB0) iD = a.diag + n0 + (int64_t)(ik + 1) * plane;
     }
 
     // stages layer ik (node plane ik + 1, element layer ik) into its ring slot (zeros outside
@@ -183,7 +194,14 @@ struct KuTile {
             const bool kin = pk >= 0 && pk < NZn;
             const uint32_t so = (uint32_t)(ik & (KU_RING - 1));
             const bool q0 = kin && r0in;
-            const T* src = q0 ? iu : a.u;
+            const T* src = q0 ? iu : src_base;
+            if (MODE == KU_CHEB0) {
+                cp_async4(s_D + so * (uint32_t)sizeof(sm.D[0]), q0 ? iD : a.diag, q0);
+                if (w == NW - 1) {
+                    const bool qn = kin && rNin;
+                    cp_async4(s_DN + so * (uint32_t)sizeof(sm.D[0]), qn ? iD + NXn : a.diag, qn);
+                }
+            }
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const uint32_t d = s_u + so * SLOT_U + c * (uint32_t)sizeof(T);
@@ -192,7 +210,7 @@ struct KuTile {
             }
             if (w == NW - 1) {  // node row je + 1 of the last warp
                 const bool qn = kin && rNin;
-                const T* srcn = qn ? iu + 3 * NXn : a.u;
+                const T* srcn = qn ? iu + 3 * NXn : src_base;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const uint32_t d = s_uN + so * SLOT_U + c * (uint32_t)sizeof(T);
@@ -207,6 +225,7 @@ struct KuTile {
         ++ik;
         iu += 3 * plane;
         iE += eplane;
+        if (MODE == KU_CHEB0) iD += plane;
     }
 
     __device__ __forceinline__ void node_pair(int slot, V3<T> (&u)[2]) const {
@@ -218,6 +237,12 @@ struct KuTile {
         u[1].xy.x = p[ROW];
         u[1].xy.y = p[ROW + 1];
         u[1].z = p[ROW + 2];
+        if (MODE == KU_CHEB0) {  // x1 = c2_0 b / diag (b is zero on non-free DOFs)
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                u[r] = (c2_0 * T(sm.D[slot][w + r][lane])) * u[r];
+            }
+        }
     }
 
     // epilogue loads of output node n (plane kk)
@@ -225,7 +250,7 @@ struct KuTile {
         e.nm = 0;
         if (emit) {
             e.nm = __ldg(a.nmask + n);
-            if (MODE == KU_RESID || MODE == KU_CHEB) {
+            if (MODE == KU_RESID || MODE == KU_CHEB || MODE == KU_CHEB0) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) e.b[c] = __ldg(a.b + 3 * n + c);
             }
@@ -287,7 +312,7 @@ struct KuTile {
 #pragma unroll
             for (int pz = 0; pz < 2; ++pz) f[0][py][pz] = f[0][py][pz] + shfl_up3(f[1][py][pz]);
         float ex = 0.f;
-        if (MODE == KU_CHEB) ex = Ee + __shfl_up_sync(FULL, Ee, 1);
+        if (Smem::CH) ex = Ee + __shfl_up_sync(FULL, Ee, 1);
         // y: corners py = 1 of warp w - 1 are corners py = 0 of warp w
         T* xo = &sm.x[par][w + 1][0][lane];
 #pragma unroll
@@ -296,7 +321,7 @@ struct KuTile {
             xo[(3 * pz + 1) * 32] = f[0][1][pz].xy.y;
             xo[(3 * pz + 2) * 32] = f[0][1][pz].z;
         }
-        if (MODE == KU_CHEB) xo[6 * 32] = T(ex);
+        if (Smem::CH) xo[6 * 32] = T(ex);
         cp_async_wait<KU_DEPTH - 1>();  // this thread's copies of layer kk + 1 have landed
         __syncthreads();                // ... everyone's, and the y hand-over is visible
         const T* xi = &sm.x[par][w][0][lane];
@@ -308,7 +333,7 @@ struct KuTile {
             r.z = xi[(3 * pz + 2) * 32];
             f[0][0][pz] = f[0][0][pz] + r;
         }
-        if (MODE == KU_CHEB) ex += (float)xi[6 * 32];
+        if (Smem::CH) ex += (float)xi[6 * 32];
         o.acc = f[0][0][1];
         o.sprev = ex;
         if (emit && owner) {
@@ -328,7 +353,7 @@ struct KuTile {
                 T* yp = a.y + 3 * n;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? ep.b[c] - y[c] : T(0);
-            } else if (MODE == KU_CHEB) {
+            } else if (Smem::CH) {
                 const float esum = in.sprev + ex;
                 const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
                 const T c1 = a.cheb ? T(a.cheb[0]) : a.c1, c2 = a.cheb ? T(a.cheb[1]) : a.c2;
@@ -338,7 +363,8 @@ struct KuTile {
                 for (int c = 0; c < 3; ++c) {
                     T dn = T(0), xn = T(0);
                     if ((nm >> c) & 1) {
-                        dn = c1 * ep.dv[c] + c2 * (ep.b[c] - y[c]) * inv;
+                        const T dprev = MODE == KU_CHEB0 ? u[c] : ep.dv[c];  // CHEB0: d_0 = x1
+                        dn = c1 * dprev + c2 * (ep.b[c] - y[c]) * inv;
                         xn = u[c] + dn;
                     }
                     dp[c] = dn;
@@ -429,10 +455,12 @@ void ku_prepare() {
     ku_resident<float, KU_APPLY_DOT>();
     ku_resident<float, KU_RESID>();
     ku_resident<float, KU_CHEB>();
+    ku_resident<float, KU_CHEB0>();
     ku_resident<double, KU_APPLY>();
     ku_resident<double, KU_APPLY_DOT>();
     ku_resident<double, KU_RESID>();
     ku_resident<double, KU_CHEB>();
+    ku_resident<double, KU_CHEB0>();
 }
 
 template <class T>
@@ -447,6 +475,7 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
         case KU_APPLY_DOT: resident = ku_resident<T, KU_APPLY_DOT>(); break;
         case KU_RESID: resident = ku_resident<T, KU_RESID>(); break;
         case KU_CHEB: resident = ku_resident<T, KU_CHEB>(); break;
+        case KU_CHEB0: resident = ku_resident<T, KU_CHEB0>(); break;
         default: return ANL_ERR_BADARG;
     }
     // one wave of CTAs. A segment costs one extra element layer, but a plane step is a
@@ -463,6 +492,7 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
         case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<blocks, block, sizeof(KuSmem<T, KU_APPLY_DOT>), s>>>(a, km); break;
         case KU_RESID: ku_kernel<T, KU_RESID><<<blocks, block, sizeof(KuSmem<T, KU_RESID>), s>>>(a, km); break;
         case KU_CHEB: ku_kernel<T, KU_CHEB><<<blocks, block, sizeof(KuSmem<T, KU_CHEB>), s>>>(a, km); break;
+        case KU_CHEB0: ku_kernel<T, KU_CHEB0><<<blocks, block, sizeof(KuSmem<T, KU_CHEB0>), s>>>(a, km); break;
         default: return ANL_ERR_BADARG;
     }
     ANL_LAUNCH_CHECK();

@@ -138,7 +138,7 @@ __global__ void k_coarsen_E(Dims f, Dims c, const float* Ef, float* Ec) {
     }
 }
 
-__global__ void k_diag(Dims d, const float* E, float kdiag, float* diag) {
+__global__ void k_diag(Dims d, const float* E, float kdiag, float* diag /* 1 / diag(K) */) {
     const int64_t nn = d.nn();
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(n % (d.nx + 1));
@@ -149,7 +149,7 @@ __global__ void k_diag(Dims d, const float* E, float kdiag, float* diag) {
             const int ei = i - 1 + (o & 1), ej = j - 1 + ((o >> 1) & 1), ek = k - 1 + ((o >> 2) & 1);
             if (ei >= 0 && ej >= 0 && ek >= 0 && ei < d.nx && ej < d.ny && ek < d.nz) s += E[d.elem(ei, ej, ek)];
         }
-        diag[n] = kdiag * s;
+        diag[n] = s > 0.f ? 1.f / (kdiag * s) : 0.f;  // the inverse diagonal, 0 where no element
     }
 }
 
@@ -216,14 +216,13 @@ __global__ void k_prolong_add(Dims f, Dims c, const T* xc, const uint8_t* nmf, T
 
 // x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
 template <class T>
-__global__ void k_cheb_first(int64_t nn, const T* b, const float* diag, const uint8_t* nmask, const double* c2p, T* x,
+__global__ void k_cheb_first(int64_t nn, const T* b, const float* dinv, const uint8_t* nmask, const double* c2p, T* x,
                              T* dv, const int* done) {
     if (done && *done) return;
     const T c2 = T(*c2p);
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
         const uint8_t m = nmask[n];
-        const float dg = diag[n];
-        const T inv = dg > 0.f ? T(1) / T(dg) : T(0);
+        const T inv = T(dinv[n]);
         for (int c = 0; c < 3; ++c) {
             const T v = (m >> c) & 1 ? c2 * b[3 * n + c] * inv : T(0);
             x[3 * n + c] = v;
@@ -622,7 +621,18 @@ template <class T>
 static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* done, cudaStream_t s) {
     const double* cf = c->cheb_d + (size_t)level_index(c, L) * kChebStride + 1;  // (c1, c2) pairs
     int k0 = 0;
-    if (x_is_zero) {
+    if (x_is_zero && degree >= 2) {  // steps 0 and 1 in one pass: x1 = c2_0 D^-1 b is never stored
+        KuArgs<T> a = ku_args<T>(c, L);
+        a.b = (const T*)L.b;
+        a.diag = L.diag;
+        a.dv = (T*)L.dv;
+        a.xout = (T*)L.x;
+        a.cheb0 = cf;
+        a.cheb = cf + 2;
+        a.done = done;
+        ANL_TRY(launch_ku<T>(KU_CHEB0, a, modal_of<T>(c), s));
+        k0 = 2;
+    } else if (x_is_zero) {
         k_cheb_first<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const T*)L.b, L.diag, L.nmask, cf + 1, (T*)L.x,
                                                          (T*)L.dv, done);
         ANL_LAUNCH_CHECK();
