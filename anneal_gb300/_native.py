@@ -33,6 +33,7 @@ EXPORTS = [
     "anl_mc_create", "anl_mc_destroy", "anl_mc_extract", "anl_mc_smooth", "anl_mc_components", "anl_mc_copy",
     "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
     "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam", "anl_element_stress",
+    "anl_vox_create", "anl_vox_destroy", "anl_voxel_fill",
 ]
 
 
@@ -81,6 +82,9 @@ _SIGS = {
     "anl_mc_components": (I, [P, P, ctypes.POINTER(I), P]),
     "anl_mc_copy": (I, [P, P, P, P]),
     "anl_mc_table": (I, [P, P]),
+    "anl_vox_create": (I, [ctypes.POINTER(P)]),
+    "anl_vox_destroy": (None, [P]),
+    "anl_voxel_fill": (I, [P, P, I64, I, I, I, D, ctypes.POINTER(D), I, P, ctypes.POINTER(I64), P]),
     "anl_nn_conv3d": (I, [P, P, P, P, P, I, I, I, I, I, I, I, I, P]),
     "anl_nn_conv3d_bwd_data": (I, [P, P, P, P, I, I, I, I, I, I, I, P]),
     "anl_nn_conv3d_bwd_weight": (I, [P, P, P, I64, P, P, I, I, I, I, I, I, I, P]),

@@ -11,6 +11,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/anneal_gb300.h"
@@ -55,6 +56,24 @@ void set_error(const char* fmt, ...);
 std::recursive_mutex& device_sync_mutex();
 void count_launch();
 void count_launches(long long n);  // kernels replayed by a CUDA graph
+
+// Grows a device buffer to at least `need` elements of `elem` bytes (contents are not kept).
+template <class P>
+inline int grow(P*& p, size_t& cap, size_t need, size_t elem) {
+    if (need <= cap) return ANL_OK;
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
+    cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const size_t n = std::max<size_t>(need, 1);
+    if (cudaMalloc((void**)&p, n * elem) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaMalloc of %zu bytes failed", n * elem);
+        return ANL_ERR_NOMEM;
+    }
+    cap = n;
+    return ANL_OK;
+}
 
 // ------------------------------------------------------------------ grid
 

@@ -5,7 +5,8 @@
 
 ``install`` swaps the reference's solve and optimise entry points for the GPU ones in the
 already imported (or importable) ``anneal`` package: ``anneal.fem.FEM`` / ``SolverError``,
-``anneal.optimize.simp`` / ``Filter``, ``anneal.export.surface``, the names ``run.py`` bound
+``anneal.optimize.simp`` / ``Filter``, ``anneal.export.surface``, the voxeliser
+(``anneal.geometry.voxel_fill`` and the name ``problem.py`` bound), the names ``run.py`` bound
 at import (``anneal.run.FEM``, ``anneal.run.simp``, ``anneal.run.surface``) and the validation
 gate's checks. Spec parsing, the other export steps, reports and the database stay the
 reference's.
@@ -39,6 +40,13 @@ def install(anneal_pkg="anneal"):
         run.surface = gexp.surface
     except ImportError:   # run.py needs trimesh / skimage / matplotlib
         pass
+    from . import geometry as ggeo
+    for mod in ("geometry", "problem"):   # problem.py:16 imports voxel_fill by name
+        try:
+            m = importlib.import_module(f"{anneal_pkg}.{mod}")
+            m.voxel_fill = ggeo.voxel_fill
+        except ImportError:   # geometry.py needs trimesh
+            pass
     try:
         val = importlib.import_module(f"{anneal_pkg}.validate")
         val.CHECKS = list(gval.CHECKS)

@@ -2,9 +2,12 @@
 
     python -m anneal_gb300.kernel_bench [--shape NX NY NZ] [--reps R] [--fp64]
     python -m anneal_gb300.kernel_bench --export [--shape NX NY NZ] [--reps R]
+    python -m anneal_gb300.kernel_bench --voxel [--shape NX NY NZ] [--reps R] [--subdiv N]
 
 --export times the iso-surface export instead: zoom (x2), classify, scan, emit, 10 Taubin
 steps and the component labels on a smooth synthetic density field.
+--voxel times the voxeliser (s = 3) on a sphere of 20 * 4^subdiv triangles filling most of the
+grid's short side (h = 1) plus a rotated box.
 
 Prints one JSON line: milliseconds per launch (CUDA events, after warm-up), the
 algorithmic bytes (24 per node + 4 per element: read u, write y, read the element
@@ -29,9 +32,13 @@ def main():
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--export", action="store_true")
+    ap.add_argument("--voxel", action="store_true")
+    ap.add_argument("--subdiv", type=int, default=6)
     a = ap.parse_args()
     if a.export:
         return export_bench(a.shape, a.reps)
+    if a.voxel:
+        return voxel_bench(a.shape, a.reps, a.subdiv)
     nx, ny, nz = a.shape
     ctx = Context((nx, ny, nz), 1.0, 0.3, fp64=a.fp64)
     ne, nn = ctx.ne, ctx.nn
@@ -84,6 +91,38 @@ def export_bench(shape, reps):
     print(json.dumps({"kernel": "iso-surface export", "shape": [nx, ny, nz], "upsample": 2, "samples": ns,
                       "vertices": nv, "faces": nf, "ms_extract": res["extract"], "ms_with_smooth_and_labels": res["all"],
                       "samples_per_s": ns / (res["extract"] * 1e-3)}))
+
+
+def voxel_tris(shape, subdiv):
+    """The voxeliser workload: a sphere (20 * 4^subdiv triangles) and a rotated box inside an
+    nx x ny x nz grid of unit elements at the origin."""
+    from . import geometry as G
+    nx, ny, nz = shape
+    r = 0.45 * min(shape)
+    V, F = G.icosphere(subdiv, r, (0.3 * nx, 0.5 * ny, 0.5 * nz))
+    rot = np.linalg.qr(np.random.default_rng(1).normal(size=(3, 3)))[0]
+    Vb, Fb = G.box((0.3 * nx, 0.5 * ny, 0.3 * nz), (0.75 * nx, 0.5 * ny, 0.5 * nz), rot)
+    return np.concatenate([V[F], Vb[Fb]])
+
+
+def voxel_bench(shape, reps, subdiv):
+    from . import geometry as G
+    tri = torch.as_tensor(voxel_tris(shape, subdiv), device="cuda")
+    vox = G.Voxeliser()
+    vox.fill_device(tri, shape, 1.0, (0.0, 0.0, 0.0), stats=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for r in range(reps + 3):
+        if r == 3:
+            e0.record()
+        f = vox.fill_device(tri, shape, 1.0, (0.0, 0.0, 0.0))
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ne = int(np.prod(shape))
+    print(json.dumps({"kernel": "voxeliser (s=3)", "shape": list(shape), "triangles": int(tri.shape[0]),
+                      "pairs": vox.pairs, "crossings": vox.hits, "ms_per_call": ms,
+                      "elements_per_s": ne / (ms * 1e-3), "fill_sum": float(f.sum())}))
+    vox.close()
 
 
 if __name__ == "__main__":

@@ -190,6 +190,24 @@ int anl_mc_copy(anl_mc* mc, float* verts, int32_t* faces, anl_stream_t stream);
    level), tri_h[256*24] their cube edges (edge 4*axis + q, q the other two corner bits). */
 int anl_mc_table(uint8_t* ntri_h, int8_t* tri_h);
 
+/* ---------------------------------------------------------------- voxeliser */
+
+/* A voxeliser workspace: device buffers that grow to the largest mesh and grid seen. Not
+   thread-safe. */
+typedef struct anl_vox anl_vox;
+int anl_vox_create(anl_vox** out);
+void anl_vox_destroy(anl_vox* vox);
+
+/* Replaces geometry.voxel_fill (geometry.py:89-149): the fill fraction (0..1) of every element
+   of the nx*ny*nz grid (spacing h, origin_h[3] on the host) inside the closed mesh tri
+   (ntri triangles x 3 vertices x xyz, FP64, device), by ray parity along z at s^3 sample
+   points per element (s in 1..16; the reference uses 3). fill: nx*ny*nz FP64 on the device,
+   x fastest. Bit-identical to the reference. stats_h (host, may be NULL; then the call does not
+   synchronise): [0] (triangle, sample column) pairs tested, [1] crossings counted.
+   ANL_ERR_BADARG for an empty mesh (the reference raises ValueError there). */
+int anl_voxel_fill(anl_vox* vox, const double* tri, int64_t ntri, int nx, int ny, int nz, double h,
+                   const double* origin_h, int s, double* fill, int64_t* stats_h, anl_stream_t stream);
+
 /* ---------------------------------------------------------------- warm-start network layers
 
    No counterpart in the reference: the reference starts each solve from the previous

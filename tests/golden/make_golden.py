@@ -266,6 +266,57 @@ def gen_stress(fem):
                         vm_scalar=model.von_mises(u, 1500.0), sn=model.normal_stress(sig, (0.2, -0.3, 1.0)))
 
 
+def gen_voxel(ref_root):
+    """geometry.voxel_fill (geometry.py:89-149) on closed meshes, an axis-aligned box whose top
+    face lies on a sample plane, a seeded triangle soup and several sub-sample counts. The
+    meshes come from anneal_gb300.geometry (icosphere, box), which stand in for
+    trimesh.creation (absent here); voxel_fill reads only ``mesh.triangles``."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import anneal.fem as fem
+    import anneal.geometry as geometry
+    from anneal_gb300 import geometry as G
+
+    class _M:
+        def __init__(self, tri):
+            self.triangles = tri
+
+    def grid_around(V, h):  # test_core.py:31-36
+        lo, hi = V.min(axis=0), V.max(axis=0)
+        return fem.Grid(np.ceil((hi - lo + 2 * h) / h).astype(int), h, lo - h)
+
+    rot = np.linalg.qr(np.random.default_rng(3).normal(size=(3, 3)))[0]
+    cases = {}
+    V, F = G.icosphere(4, 10.0)
+    cases["sphere"] = (V[F], grid_around(V, 0.75), 3)
+    V, F = G.box((5.0, 3.0, 2.0), (1.3, -0.7, 0.4), rot)
+    cases["box_rot"] = (V[F], grid_around(V, 0.5), 3)
+    V, F = G.box((3.0, 3.0, 1.5), (1.5, 1.5, 0.75))
+    cases["box_plane"] = (V[F], fem.Grid((5, 5, 4), 1.0, (-1.0, -1.0, -1.0)), 3)
+    tri = np.random.default_rng(5).uniform(-2.0, 2.0, size=(300, 3, 3))
+    cases["soup"] = (tri, fem.Grid((11, 11, 11), 0.4, (-2.2, -2.2, -2.2)), 3)
+    V, F = G.icosphere(3, 4.0, (0.3, -0.2, 0.1))
+    cases["sphere_s2"] = (V[F], grid_around(V, 0.6), 2)
+    cases["sphere_s5"] = (V[F], grid_around(V, 0.9), 5)
+    out = {}
+    for name, (tri, g, s) in cases.items():
+        out[name + "_tri"] = tri
+        out[name + "_shape"] = np.array(g.shape)
+        out[name + "_h"] = g.h
+        out[name + "_origin"] = np.asarray(g.origin, float)
+        out[name + "_s"] = s
+        out[name + "_fill"] = geometry.voxel_fill(_M(tri), g, s=s)
+    out["names"] = np.array(list(cases))
+    # a larger case kept as SHA-256 digests: the mesh (rebuilt by the test) and the fill bytes
+    import hashlib
+    V, F = G.icosphere(5, 0.45 * 64, (0.3 * 128, 32.0, 32.0))
+    g = fem.Grid((128, 64, 64), 1.0, (0.0, 0.0, 0.0))
+    fill = geometry.voxel_fill(_M(V[F]), g)
+    out["big_tri_sha256"] = hashlib.sha256(np.ascontiguousarray(V[F]).tobytes()).hexdigest()
+    out["big_fill_sha256"] = hashlib.sha256(fill.tobytes()).hexdigest()
+    out["big_fill_sum"] = fill.sum()
+    np.savez_compressed(os.path.join(HERE, "voxel.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -278,7 +329,8 @@ def main():
             "simp_small": lambda: gen_simp_small(fem, optimize),
             "simp_small_tight": lambda: gen_simp_small(fem, optimize, rtol=1e-10),
             "simp_worst": lambda: gen_simp_worst(fem, optimize),
-            "validate": lambda: gen_validate(validate), "stress": lambda: gen_stress(fem)}
+            "validate": lambda: gen_validate(validate), "stress": lambda: gen_stress(fem),
+            "voxel": lambda: gen_voxel(a.ref)}
     if not a.skip_config1:
         jobs["config1"] = lambda: gen_config1(fem, optimize)
     for name, fn in jobs.items():
