@@ -33,7 +33,8 @@ EXPORTS = [
     "anl_mc_create", "anl_mc_destroy", "anl_mc_extract", "anl_mc_smooth", "anl_mc_components", "anl_mc_copy",
     "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
     "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam", "anl_element_stress",
-    "anl_vox_create", "anl_vox_destroy", "anl_voxel_fill",
+    "anl_vox_create", "anl_vox_destroy", "anl_voxel_fill", "anl_output_field", "anl_choose_level",
+    "anl_label_above", "anl_edt",
 ]
 
 
@@ -85,6 +86,10 @@ _SIGS = {
     "anl_vox_create": (I, [ctypes.POINTER(P)]),
     "anl_vox_destroy": (None, [P]),
     "anl_voxel_fill": (I, [P, P, I64, I, I, I, D, ctypes.POINTER(D), I, P, ctypes.POINTER(I64), P]),
+    "anl_output_field": (I, [P, P, P, P, P, P, I64, P, P]),
+    "anl_choose_level": (I, [P, I64, D, D, D, I, P, P, ctypes.POINTER(D), P]),
+    "anl_label_above": (I, [P, I, I, I, D, P, P]),
+    "anl_edt": (I, [P, I, I, I, P, P, ctypes.c_size_t, P]),
     "anl_nn_conv3d": (I, [P, P, P, P, P, I, I, I, I, I, I, I, I, P]),
     "anl_nn_conv3d_bwd_data": (I, [P, P, P, P, I, I, I, I, I, I, I, P]),
     "anl_nn_conv3d_bwd_weight": (I, [P, P, P, I64, P, P, I, I, I, I, I, I, I, P]),

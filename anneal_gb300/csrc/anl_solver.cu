@@ -832,7 +832,6 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
         *relres = 0.0;
         return ANL_OK;
     }
-    const int* done = &c->sc->done;
     static const bool trace = std::getenv("ANL_TRACE") != nullptr;  // solver trace on stderr
     int last_replace = 0;
     double rr_replace = c->sc_h->rr;  // ||r||^2 at the last replacement

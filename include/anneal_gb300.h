@@ -208,6 +208,36 @@ void anl_vox_destroy(anl_vox* vox);
 int anl_voxel_fill(anl_vox* vox, const double* tri, int64_t ntri, int nx, int ny, int nz, double h,
                    const double* origin_h, int s, double* fill, int64_t* stats_h, anl_stream_t stream);
 
+/* ---------------------------------------------------------------- from design to surface */
+
+/* Replaces export.output_field (export.py:8-14): f = min(max(x fill, active ? solid_fill : 0),
+   1 - void_fill), then max(f, fill) on frozen elements. All arrays n elements on the device
+   (active, frozen: uint8 0/1). Bit-identical to the reference. */
+int anl_output_field(const double* x, const double* fill, const uint8_t* active, const double* solid_fill,
+                     const double* void_fill, const uint8_t* frozen, int64_t n, double* f, anl_stream_t stream);
+
+/* Replaces the bisection of export.choose_level (export.py:17-28): `steps` halvings of [lo, hi]
+   keeping count(f > t) > target on the low side, t = (lo + hi) / 2. f: n FP64 values on the
+   device. Eight steps per read of f. state: 2 doubles, hist: 256 uint64 of device scratch.
+   Writes the final [lo, hi] to lo_hi_h (host) and synchronises the stream; the reference's
+   level is clip((lo + hi) / 2, 0.3, 0.7). */
+int anl_choose_level(const double* f, int64_t n, double target, double lo, double hi, int steps, double* state,
+                     unsigned long long* hist, double* lo_hi_h, anl_stream_t stream);
+
+/* The connected components of {f > thr} on the nx*ny*nz grid (6-connectivity: the structure
+   ndimage.label uses in keep_load_paths, export.py:43-47). labels (int32, device): the
+   smallest element index of the element's component, -1 where f <= thr. n < 2^31. */
+int anl_label_above(const double* f, int nx, int ny, int nz, double thr, int32_t* labels, anl_stream_t stream);
+
+/* Exact Euclidean distance transform (ndimage.distance_transform_edt, as member_thickness uses
+   it, export.py:150-158): for every element the distance to the nearest element with
+   solid == 0 (unit spacing), FP64, on an nx*ny*nz grid (x fastest, each side <= 4096); pad the
+   grid with a background layer for the reference's np.pad. scratch: device memory of at least
+   align16(4 n) + 16 n + 8 max(ny nz, nx nz, nx ny) bytes. Elements with no background on the
+   grid get 1e10 (the square root of the internal infinity). */
+int anl_edt(const uint8_t* solid, int nx, int ny, int nz, double* dist, void* scratch, size_t scratch_bytes,
+            anl_stream_t stream);
+
 /* ---------------------------------------------------------------- warm-start network layers
 
    No counterpart in the reference: the reference starts each solve from the previous

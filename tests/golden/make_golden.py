@@ -317,6 +317,74 @@ def gen_voxel(ref_root):
     np.savez_compressed(os.path.join(HERE, "voxel.npz"), **out)
 
 
+def post_problem(fem, bar, seed=0):
+    """A small stand-in for the reference's Problem as export.py reads it: a 24 x 12 x 10 grid, a
+    fixed sphere anchor at x = 2 and a load sphere anchor at x = 21 joined by a bar of density
+    `bar` through a void-ish field; a keep-out slab and a frozen patch."""
+    rng = np.random.default_rng(seed)
+    g = fem.Grid((24, 12, 10), 1.0, (0.0, 0.0, 0.0))
+    c = g.elem_centers()
+    f = 0.3 * rng.random(g.nelem)
+    blob_a = np.linalg.norm(c - np.array([2.0, 6.0, 5.0]), axis=1) < 3.0
+    blob_b = np.linalg.norm(c - np.array([21.0, 6.0, 5.0]), axis=1) < 3.0
+    bar_m = (np.abs(c[:, 1] - 6.0) < 1.0) & (np.abs(c[:, 2] - 5.0) < 1.0)
+    f[blob_a | blob_b] = 0.9
+    f[bar_m & ~(blob_a | blob_b)] = bar
+    fill = np.where(rng.random(g.nelem) < 0.05, 0.5, 1.0)
+    active = ~((c[:, 2] > 8.0) & (c[:, 0] > 10.0) & (c[:, 0] < 14.0))
+    solid = np.where((c[:, 2] < 1.0) & (c[:, 0] < 3.0), 0.7, 0.0)
+    void = np.where(c[:, 2] > 9.0, 0.4, 0.0)
+    frozen = blob_a & (c[:, 0] < 1.0)
+    sdfs = [np.linalg.norm(c - np.array([2.0, 6.0, 5.0]), axis=1) - 1.5,
+            np.linalg.norm(c - np.array([21.0, 6.0, 5.0]), axis=1) - 1.5]
+    return g, dict(f=f, fill=fill, active=active, solid_fill=solid, void_fill=void, frozen=frozen,
+                   sdf_fixed=sdfs[0], sdf_load=sdfs[1], x=np.clip(f + 0.05, 0.0, 1.0))
+
+
+def gen_post(ref_root):
+    """export.output_field, choose_level and keep_load_paths (export.py:8-118) on small
+    stand-in problems: stage 1 (level lowered), stage 2 (path repair), repair off, and an
+    already connected part."""
+    import types as T
+    sk = T.ModuleType("skimage")
+    sk.measure = T.ModuleType("skimage.measure")
+    sys.modules.setdefault("skimage", sk)
+    sys.modules.setdefault("skimage.measure", sk.measure)
+    import anneal.fem as fem
+    import anneal.export as export
+    out = {}
+    cases = {"stage1": (0.45, True), "stage2": (0.2, True), "norepair": (0.2, False), "connected": (0.8, True)}
+    for name, (bar, repair) in cases.items():
+        g, d = post_problem(fem, bar)
+        prob = T.SimpleNamespace(grid=g, fill=d["fill"], active=d["active"], solid_fill=d["solid_fill"],
+                                 void_fill=d["void_fill"], frozen=d["frozen"], anchors=[
+                                     T.SimpleNamespace(name="clamp", role="fixed",
+                                                       region=T.SimpleNamespace(sdf=lambda p, s=d["sdf_fixed"]: s)),
+                                     T.SimpleNamespace(name="tip", role="load",
+                                                       region=T.SimpleNamespace(sdf=lambda p, s=d["sdf_load"]: s))])
+        fo = export.output_field(prob, d["x"])
+        level = export.choose_level(prob, d["f"], d["x"])
+        logs = []
+        f2, level2 = export.keep_load_paths(prob, d["f"], 0.5, log=logs.append, repair=repair)
+        for k, v in d.items():
+            out[f"{name}_{k}"] = v
+        out[f"{name}_output_field"] = fo
+        out[f"{name}_level"] = level
+        out[f"{name}_repair"] = repair
+        out[f"{name}_kept_f"] = f2
+        out[f"{name}_kept_level"] = level2
+        out[f"{name}_log"] = np.array(logs if logs else [""])
+    out["names"] = np.array(list(cases))
+    out["shape"] = np.array([24, 12, 10])
+    rng = np.random.default_rng(7)   # unclamped levels: targets near 0.45 and 0.62
+    for i, scale in enumerate((0.9, 0.75)):
+        lf, lx = rng.random(20000), rng.random(20000) * scale
+        lfill = np.where(rng.random(20000) < 0.1, 0.5, 1.0)
+        out[f"level{i}_f"], out[f"level{i}_x"], out[f"level{i}_fill"] = lf, lx, lfill
+        out[f"level{i}_out"] = export.choose_level(T.SimpleNamespace(fill=lfill), lf, lx)
+    np.savez_compressed(os.path.join(HERE, "post.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -330,7 +398,7 @@ def main():
             "simp_small_tight": lambda: gen_simp_small(fem, optimize, rtol=1e-10),
             "simp_worst": lambda: gen_simp_worst(fem, optimize),
             "validate": lambda: gen_validate(validate), "stress": lambda: gen_stress(fem),
-            "voxel": lambda: gen_voxel(a.ref)}
+            "voxel": lambda: gen_voxel(a.ref), "post": lambda: gen_post(a.ref)}
     if not a.skip_config1:
         jobs["config1"] = lambda: gen_config1(fem, optimize)
     for name, fn in jobs.items():
