@@ -5,13 +5,17 @@
 
 ``install`` swaps the reference's solve and optimise entry points for the GPU ones in the
 already imported (or importable) ``anneal`` package: ``anneal.fem.FEM`` / ``SolverError``,
-``anneal.optimize.simp`` / ``Filter``, ``anneal.export.surface``, the voxeliser
-(``anneal.geometry.voxel_fill`` and the name ``problem.py`` bound), the names ``run.py`` bound
-at import (``anneal.run.FEM``, ``anneal.run.simp``, ``anneal.run.surface``) and the validation
+``anneal.optimize.simp`` / ``Filter``, ``anneal.export.surface`` / ``output_field`` /
+``choose_level`` / ``keep_load_paths`` / ``member_thickness``, the voxeliser
+(``anneal.geometry.voxel_fill`` and the names ``problem.py`` and ``run.py`` bound), the names ``run.py`` bound
+at import (``anneal.run.FEM``, ``anneal.run.simp`` and the export functions) and the validation
 gate's checks. Spec parsing, the other export steps, reports and the database stay the
 reference's.
 """
 import importlib
+
+
+_EXPORT_NAMES = ("surface", "output_field", "choose_level", "keep_load_paths", "member_thickness")
 
 
 def install(anneal_pkg="anneal"):
@@ -30,18 +34,20 @@ def install(anneal_pkg="anneal"):
     from . import export as gexp
     try:
         exp = importlib.import_module(f"{anneal_pkg}.export")
-        exp.surface = gexp.surface
+        for name in _EXPORT_NAMES:
+            setattr(exp, name, getattr(gexp, name))
     except ImportError:   # export.py needs trimesh / skimage
         pass
     try:
         run = importlib.import_module(f"{anneal_pkg}.run")
         run.FEM = gfem.FEM
         run.simp = gopt.simp
-        run.surface = gexp.surface
+        for name in _EXPORT_NAMES:   # run.py:16 binds them by name
+            setattr(run, name, getattr(gexp, name))
     except ImportError:   # run.py needs trimesh / skimage / matplotlib
         pass
     from . import geometry as ggeo
-    for mod in ("geometry", "problem"):   # problem.py:16 imports voxel_fill by name
+    for mod in ("geometry", "problem", "run"):   # problem.py:16 and run.py:13 bind voxel_fill by name
         try:
             m = importlib.import_module(f"{anneal_pkg}.{mod}")
             m.voxel_fill = ggeo.voxel_fill
