@@ -155,63 +155,84 @@ __global__ void k_diag(Dims d, const float* E, float kdiag, float* diag /* 1 / d
 
 // ------------------------------------------------------------------ transfers
 
-template <class T>
-__global__ void k_restrict(Dims f, Dims c, const T* rf, const uint8_t* nmc, T* bc, const int* done) {
-    if (done && *done) return;
-    const int64_t nn = c.nn();
-    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
-        const int I = (int)(n % (c.nx + 1));
-        const int J = (int)((n / (c.nx + 1)) % (c.ny + 1));
-        const int K = (int)(n / ((int64_t)(c.nx + 1) * (c.ny + 1)));
-        T acc[3] = {T(0), T(0), T(0)};
-        for (int dk = -1; dk <= 1; ++dk) {
-            const int k = 2 * K + dk;
-            if (k < 0 || k > f.nz) continue;
-            const T wk = dk == 0 ? T(1) : T(0.5);
-            for (int dj = -1; dj <= 1; ++dj) {
-                const int j = 2 * J + dj;
-                if (j < 0 || j > f.ny) continue;
-                const T wj = dj == 0 ? wk : wk * T(0.5);
-                for (int di = -1; di <= 1; ++di) {
-                    const int i = 2 * I + di;
-                    if (i < 0 || i > f.nx) continue;
-                    const T w = di == 0 ? wj : wj * T(0.5);
-                    const int64_t fn = f.node(i, j, k);
-                    acc[0] += w * rf[3 * fn];
-                    acc[1] += w * rf[3 * fn + 1];
-                    acc[2] += w * rf[3 * fn + 2];
-                }
-            }
-        }
-        const uint8_t m = nmc[n];
-        for (int cc = 0; cc < 3; ++cc) bc[3 * n + cc] = (m >> cc) & 1 ? acc[cc] : T(0);
-    }
+// Grid transfers run one thread per output node on a 3-D launch (32 x 4 threads over x and y,
+// one z plane per block row), so no thread divides a flat index: at the finest level the
+// transfers are bound by their reads and writes.
+constexpr int TR_X = 32, TR_Y = 4;
+static inline dim3 transfer_grid(const Dims& d) {
+    return dim3((unsigned)((d.nx + 1 + TR_X - 1) / TR_X), (unsigned)((d.ny + 1 + TR_Y - 1) / TR_Y), (unsigned)(d.nz + 1));
 }
 
+// b_c = R r_f = P^T r_f (trilinear weights 1, 1/2, 1/4, 1/8), zero on fixed coarse DOFs
 template <class T>
-__global__ void k_prolong_add(Dims f, Dims c, const T* xc, const uint8_t* nmf, T* xf, const int* done) {
+__global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const T* __restrict__ rf,
+                                                          const uint8_t* __restrict__ nmc, T* __restrict__ bc,
+                                                          const int* done) {
     if (done && *done) return;
-    const int64_t nn = f.nn();
-    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(n % (f.nx + 1));
-        const int j = (int)((n / (f.nx + 1)) % (f.ny + 1));
-        const int k = (int)(n / ((int64_t)(f.nx + 1) * (f.ny + 1)));
-        const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
-        const T wi = (i & 1) ? T(0.5) : T(1), wj = (j & 1) ? T(0.5) : T(1), wk = (k & 1) ? T(0.5) : T(1);
-        T acc[3] = {T(0), T(0), T(0)};
-        for (int ck = 0; ck < nk; ++ck)
-            for (int cj = 0; cj < nj; ++cj)
-                for (int ci = 0; ci < ni; ++ci) {
-                    const int64_t cn = c.node(i / 2 + ci, j / 2 + cj, k / 2 + ck);
-                    const T w = wi * wj * wk;
-                    acc[0] += w * xc[3 * cn];
-                    acc[1] += w * xc[3 * cn + 1];
-                    acc[2] += w * xc[3 * cn + 2];
-                }
-        const uint8_t m = nmf[n];
-        for (int cc = 0; cc < 3; ++cc)
-            if ((m >> cc) & 1) xf[3 * n + cc] += acc[cc];
+    const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y, K = blockIdx.z;
+    if (I > c.nx || J > c.ny) return;
+    const int64_t fx = f.nx + 1, fxy = fx * (f.ny + 1);
+    T acc0 = T(0), acc1 = T(0), acc2 = T(0);
+#pragma unroll
+    for (int dk = -1; dk <= 1; ++dk) {
+        const int k = 2 * K + dk;
+        if (k < 0 || k > f.nz) continue;
+        const T wk = dk == 0 ? T(1) : T(0.5);
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+            const int j = 2 * J + dj;
+            if (j < 0 || j > f.ny) continue;
+            const T wj = dj == 0 ? wk : wk * T(0.5);
+            const T* row = rf + 3 * ((int64_t)k * fxy + (int64_t)j * fx);
+#pragma unroll
+            for (int di = -1; di <= 1; ++di) {
+                const int i = 2 * I + di;
+                if (i < 0 || i > f.nx) continue;
+                const T w = di == 0 ? wj : wj * T(0.5);
+                const T* q = row + 3 * i;
+                acc0 += w * __ldg(q);
+                acc1 += w * __ldg(q + 1);
+                acc2 += w * __ldg(q + 2);
+            }
+        }
     }
+    const int64_t n = (int64_t)I + (int64_t)(c.nx + 1) * ((int64_t)J + (int64_t)(c.ny + 1) * K);
+    const uint8_t m = nmc[n];
+    T* o = bc + 3 * n;
+    o[0] = (m & 1) ? acc0 : T(0);
+    o[1] = (m & 2) ? acc1 : T(0);
+    o[2] = (m & 4) ? acc2 : T(0);
+}
+
+// x_f += P x_c on free fine DOFs (trilinear interpolation of the coarse correction)
+template <class T>
+__global__ void __launch_bounds__(TR_X * TR_Y) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
+                                                             const uint8_t* __restrict__ nmf, T* __restrict__ xf,
+                                                             const int* done) {
+    if (done && *done) return;
+    const int i = blockIdx.x * TR_X + threadIdx.x, j = blockIdx.y * TR_Y + threadIdx.y, k = blockIdx.z;
+    if (i > f.nx || j > f.ny) return;
+    const int64_t n = (int64_t)i + (int64_t)(f.nx + 1) * ((int64_t)j + (int64_t)(f.ny + 1) * k);
+    const uint8_t m = nmf[n];
+    if (!(m & 7)) return;
+    const int64_t cx = c.nx + 1, cxy = cx * (c.ny + 1);
+    const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
+    const T w = ((i & 1) ? T(0.5) : T(1)) * ((j & 1) ? T(0.5) : T(1)) * ((k & 1) ? T(0.5) : T(1));
+    T acc0 = T(0), acc1 = T(0), acc2 = T(0);
+    for (int ck = 0; ck < nk; ++ck)
+        for (int cj = 0; cj < nj; ++cj) {
+            const T* row = xc + 3 * ((int64_t)(k / 2 + ck) * cxy + (int64_t)(j / 2 + cj) * cx);
+            for (int ci = 0; ci < ni; ++ci) {
+                const T* q = row + 3 * (i / 2 + ci);
+                acc0 += __ldg(q);
+                acc1 += __ldg(q + 1);
+                acc2 += __ldg(q + 2);
+            }
+        }
+    T* o = xf + 3 * n;
+    if (m & 1) o[0] += w * acc0;
+    if (m & 2) o[1] += w * acc1;
+    if (m & 4) o[2] += w * acc2;
 }
 
 // x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
@@ -674,10 +695,10 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     a.y = (T*)L.r;
     a.done = done;
     ANL_TRY(launch_ku<T>(KU_RESID, a, modal_of<T>(c), s));
-    k_restrict<T><<<vgrid(C.d.nn()), VT, 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
+    k_restrict<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<T>(c, l + 1, done, s));
-    k_prolong_add<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
+    k_prolong_add<T><<<transfer_grid(L.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(smooth<T>(c, L, c->mg_degree, false, done, s));
     return ANL_OK;

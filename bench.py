@@ -6,6 +6,10 @@ displacement, sensitivity, two filter backward passes, OC bisection, history val
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
+After W warm-up steps, K device-timed steps (design resident in HBM) alternate with K
+end-to-end steps (design copied host -> device before and device -> host after, inside the
+timed region), so both numbers sample the same SIMP iterations.
+
 N > 1 runs under torchrun with one independent replica per GPU (the solve has no
 cross-GPU exchange): value = total iterations / max rank time. ``--impl reference`` times
 the FP64 CPU oracle (the restatement of the reference's solver) on the host cores.
@@ -230,41 +234,41 @@ def run_gpu(args):
 
     barrier()
     lib = N.load()
-    launches0 = lib.anl_launch_count()
-    cg0 = len(run.fem.cg_iters)
-    total_ms = 0.0
+    # Device-timed steps and end-to-end steps alternate, so both sample the same stretch of
+    # SIMP iterations (the CG count per solve drifts as the design develops). An end-to-end
+    # step copies the current design into pinned host memory first (untimed), then times
+    # host -> device, the step and device -> host.
+    x_in = torch.empty(w.nelem, dtype=torch.float32).pin_memory()
+    x_out = torch.empty_like(x_in).pin_memory()
+    total_ms = e2e_ms = 0.0
+    launches = 0
+    cg_dev, cg_e2e = [], []
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+        for s in range(2 * args.steps):
+            device = s % 2 == 0
+            if not device:
+                x_in.copy_(run.x_t.cpu())
             flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            n0, c0 = lib.anl_launch_count(), len(run.fem.cg_iters)
             e0.record(stream)
-            run.step()
+            if device:
+                run.step()
+            else:
+                run.step_host(x_in, x_out)
             e1.record(stream)
             e1.synchronize()
-            total_ms += e0.elapsed_time(e1)
+            if device:
+                total_ms += e0.elapsed_time(e1)
+                launches += lib.anl_launch_count() - n0
+                cg_dev += run.fem.cg_iters[c0:]
+            else:
+                e2e_ms += e0.elapsed_time(e1)
+                cg_e2e += run.fem.cg_iters[c0:]
     barrier()
-    launches = lib.anl_launch_count() - launches0
-    cg_counts = run.fem.cg_iters[cg0:]
+    cg_counts = cg_dev
     value, t_max = replica_rate(total_ms, args.steps, world, "cuda")
-
-    # end to end: the design goes host -> device -> host around every step (pinned buffers)
-    x_in = torch.empty(w.nelem, dtype=torch.float32).pin_memory()
-    x_out = torch.empty_like(x_in).pin_memory()
-    x_in.copy_(run.x_t.cpu())
-    e2e_ms = 0.0
-    barrier()
-    for _ in range(args.steps):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        run.step_host(x_in, x_out)
-        e1.record(stream)
-        e1.synchronize()
-        e2e_ms += e0.elapsed_time(e1)
-        x_in.copy_(x_out)
-    barrier()
     e2e, e2e_ms = replica_rate(e2e_ms, args.steps, world, "cuda")
 
     # dominant kernel: the fine-level K u, timed alone with CUDA events on this stream
@@ -288,6 +292,7 @@ def run_gpu(args):
                         "d2h_bytes_per_step": 4 * w.nelem},
                 "gpu_launches": int(launches),
                 "cg_iters_per_solve": float(np.mean(cg_counts)) if cg_counts else None,
+                "cg_iters_per_solve_e2e": float(np.mean(cg_e2e)) if cg_e2e else None,
                 "roofline": {"kernel": "ku_kernel<float,APPLY> (fine-level K u)", "bound": "hbm",
                              "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                              "peak_kind": peak_kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
