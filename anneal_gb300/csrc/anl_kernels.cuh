@@ -25,6 +25,7 @@ struct KuArgs {
     T c1 = T(0), c2 = T(0);          // CHEB: d <- c1 d + c2 D^-1 (b - K u)
     const double* cheb = nullptr;    // CHEB: {c1, c2} in device memory (overrides c1, c2)
     int c1_zero = 0;                 // CHEB: first step of a sweep (c1 = 0, d is not read)
+    int dv_keep = 1;                 // CHEB, CHEB0: 0 on the last step of a sweep (d is not stored)
     const double* cheb0 = nullptr;   // CHEB0: {c1_0, c2_0} of the step from x = 0
     const float* diag = nullptr;     // CHEB0: inverse diagonal of K per node (0 where unused)
     T kdiag = T(0);                  // diagonal entry of Ke(1) (all 24 are equal)

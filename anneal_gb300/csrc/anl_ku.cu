@@ -93,6 +93,7 @@ struct KuCarry {
     V3<T> dxb[2];  // Dx of rows je, je + 1
     V3<T> dyb[2];  // Dy of columns ie, ie + 1
     V3<T> acc;     // forces of the layer below on node (ie, je)
+    V3<T> braw;    // CHEB0: b at node (ie, je), as staged (before the D^-1 scaling)
     float sprev;   // E summed over the 4 elements of the layer below around node (ie, je)
 };
 // epilogue inputs of the next output node, loaded one layer ahead
@@ -228,7 +229,7 @@ struct KuTile {
         if (MODE == KU_CHEB0) iD += plane;
     }
 
-    __device__ __forceinline__ void node_pair(int slot, V3<T> (&u)[2]) const {
+    __device__ __forceinline__ void node_pair(int slot, V3<T> (&u)[2], V3<T>* raw0 = nullptr) const {
         const T* p = &sm.u[slot][w][lane][0];
         constexpr int ROW = 32 * 3;
         u[0].xy.x = p[0];
@@ -238,6 +239,7 @@ struct KuTile {
         u[1].xy.y = p[ROW + 1];
         u[1].z = p[ROW + 2];
         if (MODE == KU_CHEB0) {  // x1 = c2_0 b / diag (b is zero on non-free DOFs)
+            if (raw0) *raw0 = u[0];
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 u[r] = (c2_0 * T(sm.D[slot][w + r][lane])) * u[r];
@@ -250,7 +252,7 @@ struct KuTile {
         e.nm = 0;
         if (emit) {
             e.nm = __ldg(a.nmask + n);
-            if (MODE == KU_RESID || MODE == KU_CHEB || MODE == KU_CHEB0) {
+            if (MODE == KU_RESID || MODE == KU_CHEB) {  // CHEB0 has b staged already
 #pragma unroll
                 for (int c = 0; c < 3; ++c) e.b[c] = __ldg(a.b + 3 * n + c);
             }
@@ -263,7 +265,7 @@ struct KuTile {
 
     // carry of the node plane staged in `slot` (edge differences only, no forces yet)
     __device__ __forceinline__ void start(int slot, KuCarry<T>& c) const {
-        node_pair(slot, c.ub);
+        node_pair(slot, c.ub, &c.braw);
         const V3<T> nb0 = shfl_down3(c.ub[0]), nb1 = shfl_down3(c.ub[1]);
         c.dxb[0] = nb0 - c.ub[0];
         c.dxb[1] = nb1 - c.ub[1];
@@ -283,7 +285,7 @@ struct KuTile {
         issue_next(kend);
         epi_load(n + plane, owner && kk + 1 < kend, epn);
         V3<T> cu[2];
-        node_pair(slot, cu);
+        node_pair(slot, cu, &o.braw);
         const float Ee = sm.E[slot][w][lane];
         // edge differences of the upper plane
         const V3<T> un0 = shfl_down3(cu[0]), un1 = shfl_down3(cu[1]);
@@ -340,6 +342,8 @@ struct KuTile {
             const V3<T> yv = in.acc + f[0][0][0];
             const T y[3] = {yv.xy.x, yv.xy.y, yv.z};
             const T u[3] = {in.ub[0].xy.x, in.ub[0].xy.y, in.ub[0].z};
+            const T b[3] = {MODE == KU_CHEB0 ? in.braw.xy.x : ep.b[0], MODE == KU_CHEB0 ? in.braw.xy.y : ep.b[1],
+                            MODE == KU_CHEB0 ? in.braw.z : ep.b[2]};
             const uint8_t nm = ep.nm;
             if (MODE == KU_APPLY || MODE == KU_APPLY_DOT) {
                 T* yp = a.y + 3 * n;
@@ -352,7 +356,7 @@ struct KuTile {
             } else if (MODE == KU_RESID) {
                 T* yp = a.y + 3 * n;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? ep.b[c] - y[c] : T(0);
+                for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? b[c] - y[c] : T(0);
             } else if (Smem::CH) {
                 const float esum = in.sprev + ex;
                 const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
@@ -364,10 +368,10 @@ struct KuTile {
                     T dn = T(0), xn = T(0);
                     if ((nm >> c) & 1) {
                         const T dprev = MODE == KU_CHEB0 ? u[c] : ep.dv[c];  // CHEB0: d_0 = x1
-                        dn = c1 * dprev + c2 * (ep.b[c] - y[c]) * inv;
+                        dn = c1 * dprev + c2 * (b[c] - y[c]) * inv;
                         xn = u[c] + dn;
                     }
-                    dp[c] = dn;
+                    if (a.dv_keep) dp[c] = dn;
                     xp[c] = xn;
                 }
             }

@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
 
 // x_f += P x_c on free fine DOFs (trilinear interpolation of the coarse correction)
 template <class T>
-__global__ void __launch_bounds__(TR_X * TR_Y) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
+__global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
                                                              const uint8_t* __restrict__ nmf, T* __restrict__ xf,
                                                              const int* done) {
     if (done && *done) return;
@@ -444,6 +444,33 @@ __global__ void k_init_scalars(PcgScalars* sc, double rtol, int maxiter, const d
     sc->pq = 0.0;
 }
 
+// Four consecutive entries per access (16-byte loads and stores; every vector of the CG and
+// the hierarchy starts on a 256-byte cudaMalloc boundary). The CG kernels walk the vectors in
+// groups of four; the last n % 4 entries go to a scalar tail.
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+// calls f(i) for every index of [0, n) this thread owns: groups of four, then the tail
+template <class F4, class F1>
+__device__ __forceinline__ void for_each4(int64_t n, F4 f4, F1 f1) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x, t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t n4 = n >> 2;
+    for (int64_t g = t; g < n4; g += stride) f4(4 * g);
+    for (int64_t i = 4 * n4 + t; i < n; i += stride) f1(i);
+}
+
 template <class T>
 __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgScalars* sc, const int* restart,
                              double* partials, unsigned* counter) {
@@ -451,11 +478,25 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
     if (sc->done) return;
     const bool rs = *restart != 0;
     Sum<T> a, b;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const T zi = z[i];
-        a.prod(r[i], zi);
-        if (!rs) b.prod(zi, q[i]);
-    }
+    for_each4(
+        n,
+        [&](int64_t i) {
+            T zv[4], rv[4], qv[4];
+            ld4(z + i, zv);
+            ld4(r + i, rv);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) a.prod(rv[e], zv[e]);
+            if (!rs) {
+                ld4(q + i, qv);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) b.prod(zv[e], qv[e]);
+            }
+        },
+        [&](int64_t i) {
+            const T zi = z[i];
+            a.prod(r[i], zi);
+            if (!rs) b.prod(zi, q[i]);
+        });
     double v[2] = {a.get(), b.get()};
     block_sum<2, VT>(v, sm, threadIdx.x);
     __shared__ double res[2];
@@ -478,14 +519,29 @@ template <class T>
 __global__ void k_pupdate(int64_t n, const T* z, T* p, const PcgScalars* sc, const int* restart) {
     if (sc->done) return;
     const int it = sc->iters;
-    if (*restart) {
-        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = z[i];
+    if (*restart) {  // p = z (not z + 0 p: p may hold non-finite values after a breakdown)
+        for_each4(
+            n,
+            [&](int64_t i) {
+                T zv[4];
+                ld4(z + i, zv);
+                st4(p + i, zv);
+            },
+            [&](int64_t i) { p[i] = z[i]; });
         return;
     }
-    const double beta = -sc->alpha * sc->zq / sc->rz[(it + 1) & 1];
-    const T bt = T(beta);
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = z[i] + bt * p[i];
+    const T bt = T(-sc->alpha * sc->zq / sc->rz[(it + 1) & 1]);
+    for_each4(
+        n,
+        [&](int64_t i) {
+            T zv[4], pv[4];
+            ld4(z + i, zv);
+            ld4(p + i, pv);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) pv[e] = zv[e] + bt * pv[e];
+            st4(p + i, pv);
+        },
+        [&](int64_t i) { p[i] = z[i] + bt * p[i]; });
 }
 
 constexpr double kRecurrenceMargin = 0.5;  // (0.71 rtol)^2: the recurrence target, squared
@@ -502,13 +558,30 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
     Sum<T> rr;
     if (!bad) {
         const T at = T(alpha);
-        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-            const T pi = p[i];
-            x[i] = fma(alpha, (double)pi, x[i]);
-            const T ri = r[i] - at * q[i];
-            r[i] = ri;
-            rr.prod(ri, ri);
-        }
+        for_each4(
+            n,
+            [&](int64_t i) {
+                T pv[4], qv[4], rv[4];
+                double xv[4];
+                ld4(p + i, pv);
+                ld4(q + i, qv);
+                ld4(r + i, rv);
+                ld4(x + i, xv);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    xv[e] = fma(alpha, (double)pv[e], xv[e]);
+                    rv[e] = rv[e] - at * qv[e];
+                    rr.prod(rv[e], rv[e]);
+                }
+                st4(x + i, xv);
+                st4(r + i, rv);
+            },
+            [&](int64_t i) {
+                x[i] = fma(alpha, (double)p[i], x[i]);
+                const T ri = r[i] - at * q[i];
+                r[i] = ri;
+                rr.prod(ri, ri);
+            });
     }
     double v[1] = {rr.get()};
     block_sum<1, VT>(v, sm, threadIdx.x);
@@ -650,6 +723,7 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
         a.xout = (T*)L.x;
         a.cheb0 = cf;
         a.cheb = cf + 2;
+        a.dv_keep = degree > 2;
         a.done = done;
         ANL_TRY(launch_ku<T>(KU_CHEB0, a, modal_of<T>(c), s));
         k0 = 2;
@@ -667,6 +741,7 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
         a.xout = (T*)L.xt;
         a.cheb = cf + 2 * k;
         a.c1_zero = k == 0;
+        a.dv_keep = k + 1 < degree;
         a.done = done;
         ANL_TRY(launch_ku<T>(KU_CHEB, a, modal_of<T>(c), s));
         std::swap(L.x, L.xt);
