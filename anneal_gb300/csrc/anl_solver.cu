@@ -204,35 +204,70 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
     o[2] = (m & 4) ? acc2 : T(0);
 }
 
-// x_f += P x_c on free fine DOFs (trilinear interpolation of the coarse correction)
+// x_f += P x_c on free fine DOFs (trilinear interpolation of the coarse correction). One
+// thread per coarse node (I, J, K) updates the up to 8 fine nodes (2I + a, 2J + b, 2K + g),
+// a, b, g in {0, 1}, from the up to 8 coarse nodes (I + a', J + b', K + g'): every load of a
+// thread is independent of the others, so the loads of a warp overlap.
 template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
-                                                             const uint8_t* __restrict__ nmf, T* __restrict__ xf,
-                                                             const int* done) {
+                                                                const uint8_t* __restrict__ nmf, T* __restrict__ xf,
+                                                                const int* done) {
     if (done && *done) return;
-    const int i = blockIdx.x * TR_X + threadIdx.x, j = blockIdx.y * TR_Y + threadIdx.y, k = blockIdx.z;
-    if (i > f.nx || j > f.ny) return;
-    const int64_t n = (int64_t)i + (int64_t)(f.nx + 1) * ((int64_t)j + (int64_t)(f.ny + 1) * k);
-    const uint8_t m = nmf[n];
-    if (!(m & 7)) return;
+    const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y, K = blockIdx.z;
+    if (I > c.nx || J > c.ny) return;
     const int64_t cx = c.nx + 1, cxy = cx * (c.ny + 1);
-    const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
-    const T w = ((i & 1) ? T(0.5) : T(1)) * ((j & 1) ? T(0.5) : T(1)) * ((k & 1) ? T(0.5) : T(1));
-    T acc0 = T(0), acc1 = T(0), acc2 = T(0);
-    for (int ck = 0; ck < nk; ++ck)
-        for (int cj = 0; cj < nj; ++cj) {
-            const T* row = xc + 3 * ((int64_t)(k / 2 + ck) * cxy + (int64_t)(j / 2 + cj) * cx);
-            for (int ci = 0; ci < ni; ++ci) {
-                const T* q = row + 3 * (i / 2 + ci);
-                acc0 += __ldg(q);
-                acc1 += __ldg(q + 1);
-                acc2 += __ldg(q + 2);
+    const int64_t fx = f.nx + 1, fxy = fx * (f.ny + 1);
+    // coarse corner values v[g][b][a] (zero beyond the coarse grid: never used with weight)
+    T v[2][2][2][3];
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+        for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const bool in = I + a <= c.nx && J + bb <= c.ny && K + g <= c.nz;
+                const T* q = xc + 3 * ((int64_t)(K + g) * cxy + (int64_t)(J + bb) * cx + (I + a));
+#pragma unroll
+                for (int e = 0; e < 3; ++e) v[g][bb][a][e] = in ? __ldg(q + e) : T(0);
+            }
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+        const int k = 2 * K + g;
+        if (k > f.nz) continue;
+#pragma unroll
+        for (int bb = 0; bb < 2; ++bb) {
+            const int j = 2 * J + bb;
+            if (j > f.ny) continue;
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const int i = 2 * I + a;
+                if (i > f.nx) continue;
+                const int64_t n = (int64_t)k * fxy + (int64_t)j * fx + i;
+                const uint8_t m = nmf[n];
+                if (!(m & 7)) continue;
+                // fine node (i, j, k): the mean of the coarse nodes it lies between
+                T acc[3];
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    T t = v[0][0][0][e];
+                    if (a) t += v[0][0][1][e];
+                    if (bb) t += v[0][1][0][e] + (a ? v[0][1][1][e] : T(0));
+                    if (g) {
+                        T u = v[1][0][0][e];
+                        if (a) u += v[1][0][1][e];
+                        if (bb) u += v[1][1][0][e] + (a ? v[1][1][1][e] : T(0));
+                        t += u;
+                    }
+                    acc[e] = t;
+                }
+                const T w = (a ? T(0.5) : T(1)) * (bb ? T(0.5) : T(1)) * (g ? T(0.5) : T(1));
+                T* o = xf + 3 * n;
+                if (m & 1) o[0] += w * acc[0];
+                if (m & 2) o[1] += w * acc[1];
+                if (m & 4) o[2] += w * acc[2];
             }
         }
-    T* o = xf + 3 * n;
-    if (m & 1) o[0] += w * acc0;
-    if (m & 2) o[1] += w * acc1;
-    if (m & 4) o[2] += w * acc2;
+    }
 }
 
 // x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
@@ -773,7 +808,7 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     k_restrict<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<T>(c, l + 1, done, s));
-    k_prolong_add<T><<<transfer_grid(L.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
+    k_prolong_add<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(smooth<T>(c, L, c->mg_degree, false, done, s));
     return ANL_OK;
