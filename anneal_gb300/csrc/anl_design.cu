@@ -417,20 +417,35 @@ __global__ void k_oc_scale(int64_t ne, const uint8_t* active, const uint8_t* fro
 }
 
 // With no projection the volume is linear in xn: vol = sum_j wv_j xn_j + sum_frozen phi,
-// wv = Filter.backward(phi on non-frozen elements). One pass per bisection step.
-__global__ void k_oc_vol_linear(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x,
-                                const float* dcx, const float* dvx, const float* wv, float lam, float move,
-                                double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[DT / 32];
-    Acc2 acc;
+// wv = Filter.backward(phi on non-frozen elements). One pass evaluates a bank of up to OC_BANK
+// lambdas, the nodes of OC_BANK_DEPTH consecutive bisection steps; each volume is its own
+// deterministic two-stage sum, so the bisection takes the decisions a pass per step would.
+constexpr int OC_BANK_DEPTH = 3;
+constexpr int OC_BANK = (1 << OC_BANK_DEPTH) - 1;
+static_assert(OC_BANK <= kMaxRedVals, "one partial per lambda and block");
+struct OcBank {
+    float lam[OC_BANK];
+    int n;
+};
+
+__global__ void k_oc_vol_bank(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x,
+                              const float* dcx, const float* dvx, const float* wv, OcBank bank, float move,
+                              double* partials, unsigned* counter, double* out) {
+    __shared__ double sm[OC_BANK * DT / 32];
+    Acc2 acc[OC_BANK];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
         if (active[e]) {
-            const float xn = frozen[e] ? 1.f : oc_xn(x[e], dcx[e], dvx[e], lam, move);
-            acc.add_prod(wv[e], xn);
+            const bool fz = frozen[e] != 0;
+            const float xe = x[e], ce = dcx[e], ve = dvx[e], we = wv[e];
+#pragma unroll
+            for (int j = 0; j < OC_BANK; ++j)
+                if (j < bank.n) acc[j].add_prod(we, fz ? 1.f : oc_xn(xe, ce, ve, bank.lam[j], move));
         }
-    double v[1] = {acc.value()};
-    block_sum<1, DT>(v, sm, threadIdx.x);
-    finish_reduction<1, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
+    double v[OC_BANK];
+#pragma unroll
+    for (int j = 0; j < OC_BANK; ++j) v[j] = acc[j].value();
+    block_sum<OC_BANK, DT>(v, sm, threadIdx.x);
+    finish_reduction<OC_BANK, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,
@@ -485,35 +500,76 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
     }
     double lam = std::sqrt(lo * hi);
     int steps = 0;
-    for (int k = 0; k < 100; ++k) {
-        lam = std::sqrt(lo * hi);
-        double vol;
-        if (linear) {
-            k_oc_vol_linear<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, c->ftmp, (float)lam, (float)mv,
-                                                     c->partials, c->counter, c->red_out);
-            ANL_LAUNCH_CHECK();
-            ANL_TRY(read_red(c, 1, s));
-            vol = c->red_h[0] + vfrozen;
-        } else {
-            FilterArgs a{};
-            a.frozen = frozen;
-            a.beta = (float)beta;
-            a.eta = (float)eta;
-            a.t0 = (float)std::tanh(beta * eta);
-            a.t1 = (float)std::tanh(beta * (1 - eta));
-            a.x = x;
-            a.dcx = dcx;
-            a.dvx = dvx;
-            a.phi = phi;
-            a.lam = (float)lam;
-            a.move = (float)mv;
-            a.partials = c->partials;
-            a.counter = c->counter;
-            a.red_out = c->red_out;
-            ANL_TRY(launch_filter(c, F_OCVOL, a, s));
-            ANL_TRY(read_red(c, 1, s));
-            vol = c->red_h[0];
+    // linear volume: OC_BANK_DEPTH bisection steps per pass over the design
+    while (linear && steps < 100) {
+        const int depth = std::min(OC_BANK_DEPTH, 100 - steps);
+        const int nodes = (1 << depth) - 1, root = (1 << (depth - 1)) - 1;
+        OcBank bank{};
+        bank.n = nodes;
+        for (int j = 0; j < nodes; ++j) {  // node j (in order): lambda on the path from the root
+            double l = lo, h = hi;
+            int idx = root, step = depth >= 2 ? 1 << (depth - 2) : 0;
+            while (true) {
+                const double t = std::sqrt(l * h);
+                if (j == idx) {
+                    bank.lam[j] = (float)t;
+                    break;
+                }
+                if (j > idx) {
+                    l = t;
+                    idx += step;
+                } else {
+                    h = t;
+                    idx -= step;
+                }
+                step >>= 1;
+            }
         }
+        k_oc_vol_bank<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, c->ftmp, bank, (float)mv,
+                                               c->partials, c->counter, c->red_out);
+        ANL_LAUNCH_CHECK();
+        ANL_TRY(read_red(c, nodes, s));
+        bool stop = false;
+        int idx = root, step = depth >= 2 ? 1 << (depth - 2) : 0;
+        for (int d = 0; d < depth; ++d) {  // optimize.py:147-160, one step per level of the bank
+            lam = std::sqrt(lo * hi);
+            const double vol = c->red_h[idx] + vfrozen;
+            if (vol > vtarget) {
+                lo = lam;
+                idx += step;
+            } else {
+                hi = lam;
+                idx -= step;
+            }
+            step >>= 1;
+            ++steps;
+            if (hi / lo < 1 + 1e-9) {
+                stop = true;
+                break;
+            }
+        }
+        if (stop) break;
+    }
+    for (int k = 0; k < 100 && !linear; ++k) {  // projected volume: one filter pass per step
+        lam = std::sqrt(lo * hi);
+        FilterArgs a{};
+        a.frozen = frozen;
+        a.beta = (float)beta;
+        a.eta = (float)eta;
+        a.t0 = (float)std::tanh(beta * eta);
+        a.t1 = (float)std::tanh(beta * (1 - eta));
+        a.x = x;
+        a.dcx = dcx;
+        a.dvx = dvx;
+        a.phi = phi;
+        a.lam = (float)lam;
+        a.move = (float)mv;
+        a.partials = c->partials;
+        a.counter = c->counter;
+        a.red_out = c->red_out;
+        ANL_TRY(launch_filter(c, F_OCVOL, a, s));
+        ANL_TRY(read_red(c, 1, s));
+        const double vol = c->red_h[0];
         if (vol > vtarget) lo = lam;
         else hi = lam;
         ++steps;
