@@ -992,21 +992,22 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
         }
         // Replace the recurrence residual by the true one when the recurrence claims
         // convergence, runs out of iterations or breaks down, every 50 iterations, and
-        // whenever ||r|| has dropped 1000x since the last replacement (reliable updates).
+        // whenever ||r|| has dropped 1000x since the last replacement (reliable updates),
+        // unless it is already within 10 rtol: the certification follows a few iterations
+        // later and replaces it then.
         const bool want_check = h.done == 1 || h.done == 2 || h.done == 4 || h.iters - last_replace >= 50 ||
-                                h.rr <= 1e-6 * rr_replace;
+                                (h.rr <= 1e-6 * rr_replace && h.rr > 100.0 * h.tol2);
         if (!want_check) continue;
-        // certify with the accurate residual when the recurrence claims convergence or
-        // stops; the periodic replacements only need the cheap one
-        const bool certify = h.done == 1 || h.done == 2 || h.done == 4;
-        ANL_TRY(true_residual<T>(c, 1, s, certify));
+        // Every replacement takes the accurate residual of the FP64 element blocks. The FP32
+        // operator differs from them by a few eps in every element force, which leaves a
+        // residual of several rtol in high-frequency modes at the end of an FP32 recurrence.
+        // Taking the accurate residual already at the mid-solve replacement lets the
+        // iteration remove that part on the way, so the final certification passes at the
+        // first attempt (with the plain residual there, the first certification failed in
+        // every solve and cost a second certification and two more iterations).
+        ANL_TRY(true_residual<T>(c, 1, s, true));
         ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
         ANL_CUDA(cudaStreamSynchronize(s));
-        if (!certify && c->sc_h->done == 1) {  // the cheap residual may not certify: recheck
-            ANL_TRY(true_residual<T>(c, 1, s, true));
-            ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
-            ANL_CUDA(cudaStreamSynchronize(s));
-        }
         const PcgScalars& t = *c->sc_h;
         if (trace)
             std::fprintf(stderr, "[anl cg] it %d state %d rec %.3e true %.3e (rel, tol %.1e)\n", t.iters, h.done,
