@@ -232,6 +232,7 @@ static void free_ctx(anl_ctx* c) {
     f(c->p);
     f(c->q);
     f(c->xhi);
+    f(c->xdf);
     f(c->xlo);
     f(c->y1);
     f(c->y2);
@@ -274,11 +275,6 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         free_ctx(c);
         return ANL_ERR_BADARG;
     }
-    for (int a = 0; a < 8; ++a)
-        for (int t = 0; t < 9; ++t) {
-            c->kbf.blk[a][t] = (float)c->kbd.blk[a][t];
-            c->kbf_lo.blk[a][t] = (float)(c->kbd.blk[a][t] - (double)c->kbf.blk[a][t]);
-        }
     const double mdev = ke_modal(c->ke, &c->kmd);
     if (!(mdev < 1e-12)) {
         set_error("element matrix lacks the isotropic mode structure (deviation %g)", mdev);
@@ -287,6 +283,8 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     }
     c->kmf = KeModal<float>{(float)c->kmd.ab, (float)c->kmd.b, (float)c->kmd.c,  (float)c->kmd.d,
                             (float)c->kmd.f,  (float)c->kmd.gh, (float)c->kmd.h, (float)c->kmd.j};
+    c->kmdf = KeModal<DF>{DF(c->kmd.ab), DF(c->kmd.b), DF(c->kmd.c),  DF(c->kmd.d),
+                          DF(c->kmd.f),  DF(c->kmd.gh), DF(c->kmd.h), DF(c->kmd.j)};
     c->kdiag = c->ke[0];
     {  // largest eigenvalue of Ke by power iteration in FP64 (Ke is positive semidefinite)
         double v[24], w[24], lam = 0.0;
@@ -365,6 +363,7 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     ALLOC(c->q, 3 * nn * ts);
     ALLOC(c->xhi, 3 * nn * ts);
     ALLOC(c->xlo, 3 * nn * ts);
+    if (!c->fp64) ALLOC(c->xdf, 3 * nn * sizeof(DF));
     ALLOC(c->y1, 3 * nn * ts);
     ALLOC(c->y2, 3 * nn * ts);
     ALLOC(c->tmp, 3 * nn * ts);

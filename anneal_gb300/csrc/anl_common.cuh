@@ -375,6 +375,55 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// A double-float: the unevaluated sum hi + lo of two floats, about 48 significant bits.
+// Sums and products cost a few FP32 instructions (TwoSum, FMA-based TwoProd), far less than
+// FP64 arithmetic on this part. Used for the accurate residual of the FP64 operator.
+struct alignas(8) DF {
+    float hi, lo;
+    DF() = default;
+    __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ constexpr DF(float v) : hi(v), lo(0.f) {}
+    __host__ __device__ explicit constexpr DF(int v) : hi((float)v), lo(0.f) {}
+    __host__ __device__ explicit DF(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+    __host__ __device__ explicit operator float() const { return hi + lo; }
+    __host__ __device__ double value() const { return (double)hi + (double)lo; }
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ DF df_norm(float s, float e) {  // |s| >= |e|
+    const float h = s + e;
+    return DF(h, e - (h - s));
+}
+__device__ __forceinline__ DF operator+(DF a, DF b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    return df_norm(s, e);
+}
+__device__ __forceinline__ DF operator-(DF a, DF b) { return a + DF(-b.hi, -b.lo); }
+__device__ __forceinline__ DF operator*(DF a, DF b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ DF operator/(DF a, DF b) { return DF(a.value() / b.value()); }  // not on a hot path
+__device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
+__device__ __forceinline__ bool operator>(DF a, DF b) { return a.value() > b.value(); }
+#endif
+struct dfpair {
+    DF x, y;
+};
+template <>
+struct PairOf<DF> {
+    using type = dfpair;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ dfpair padd(dfpair a, dfpair b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ dfpair psub(dfpair a, dfpair b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ dfpair pscale(DF s, dfpair a) { return {s * a.x, s * a.y}; }
+#endif
+
 // Compensated accumulator: adds a*b exactly up to FP32 rounding of the error terms.
 struct Acc2 {
     float s = 0.f, c = 0.f;

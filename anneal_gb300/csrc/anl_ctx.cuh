@@ -47,11 +47,10 @@ struct anl_ctx {
 
     double ke[576];                 // Ke(1) row-major (host)
     double* ke_d = nullptr;         // Ke(1) on the device (coarse assembly)
-    anl::KeBlocks<double> kbd{};
-    anl::KeBlocks<float> kbf{};
-    anl::KeBlocks<float> kbf_lo{};  // kbd - kbf: with kbf, the FP64 blocks as float pairs
+    anl::KeBlocks<double> kbd{};  // the reflection structure of Ke (checked at creation)
     anl::KeModal<double> kmd{};
     anl::KeModal<float> kmf{};
+    anl::KeModal<anl::DF> kmdf{};  // kmd as double-floats (the accurate residual)
     double kdiag = 0.0;
     // lambda_max(Ke) / Ke_00 >= lambda_max(D^-1 K) for every field of element scales (the
     // element-by-element bound: x.Kx = sum_e E_e x_e.Ke x_e <= bound sum_e E_e Ke_00 |x_e|^2)
@@ -82,6 +81,7 @@ struct anl_ctx {
     void* q = nullptr;
     void* xhi = nullptr;
     void* xlo = nullptr;
+    void* xdf = nullptr;  // FP32 mode: x as (hi, lo) float pairs for the accurate residual
     void* y1 = nullptr;
     void* y2 = nullptr;
     void* tmp = nullptr;

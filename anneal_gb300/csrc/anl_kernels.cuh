@@ -38,23 +38,7 @@ struct KuArgs {
 
 template <class T>
 int launch_ku(int mode, const KuArgs<T>& a, const KeModal<T>& km, cudaStream_t s);
+int launch_ku_resid_df(const KuArgs<DF>& a, const KeModal<DF>& km, cudaStream_t s);
 
-// r = b - K32 x with x = xhi + xlo, evaluated in float-pair arithmetic; ||r||^2 -> *rr_out
-struct ResidHpArgs {
-    Dims d;
-    int kz = 0;
-    const float* E = nullptr;
-    const uint8_t* nmask = nullptr;
-    const float* xhi = nullptr;
-    const float* xlo = nullptr;
-    const double* b = nullptr;
-    float* r = nullptr;
-    double* partials = nullptr;
-    unsigned* counter = nullptr;
-    int partial_capacity = 0;
-    double* rr_out = nullptr;
-};
-// kb + kbl: the FP64 element blocks as float pairs (hi, lo)
-int launch_resid_hp(const ResidHpArgs& a, const KeBlocks<float>& kb, const KeBlocks<float>& kbl, cudaStream_t s);
 
 }  // namespace anl

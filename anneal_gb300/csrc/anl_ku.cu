@@ -16,18 +16,18 @@
 // at NW = 16). Edge differences of the lower node plane are carried from the previous layer,
 // and warps whose 32 elements are all void skip the element arithmetic.
 // HBM traffic is u once, y once, E once and the node mask once (halo re-reads hit L2).
+//
+// The same kernel in double-float arithmetic (T = DF, residual mode only) evaluates the FP64
+// operator's residual b - K x for the FP32 solver's certification: every difference, product
+// and sum is an unevaluated float pair, accurate to about 2^-48 of the terms, at a fraction
+// of the cost of FP64 arithmetic on this part.
 #include <algorithm>
+#include <type_traits>
 
 #include "anl_common.cuh"
 #include "anl_kernels.cuh"
 
 namespace anl {
-
-// the 32x8 tile of the float-pair residual kernel below
-constexpr int KU_BX = 32, KU_BY = 8;
-constexpr int KU_HX = KU_BX + 2, KU_HY = KU_BY + 2;
-constexpr int KU_EX = KU_BX + 1, KU_EY = KU_BY + 1;
-constexpr int KU_NT = KU_BX * KU_BY;
 
 #ifndef KU_NW32
 #define KU_NW32 16  // warps per CTA of the FP32 K u kernel
@@ -56,6 +56,26 @@ struct DotAcc<double> {
     __device__ void add(double x, double y) { s = fma(x, y, s); }
     __device__ double value() const { return s; }
 };
+template <>
+struct DotAcc<DF> {  // the accurate residual: ||r||^2 in FP64
+    double s = 0.0;
+    __device__ void add(DF x, DF y) { s = fma(x.value(), y.value(), s); }
+    __device__ void add_sq(double v) { s = fma(v, v, s); }
+    __device__ double value() const { return s; }
+};
+
+// node-field loads of the epilogue; the double-float residual reads its right-hand side from
+// an FP64 vector and splits it
+__device__ __forceinline__ float ldg_t(const float* p) { return __ldg(p); }
+__device__ __forceinline__ double ldg_t(const double* p) { return __ldg(p); }
+__device__ __forceinline__ DF ldg_t(const DF* p) { return DF(__ldg(reinterpret_cast<const double*>(p))); }
+
+__device__ __forceinline__ float shfl_dn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ double shfl_dn(double v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ DF shfl_dn(DF v) { return DF(shfl_dn(v.hi), shfl_dn(v.lo)); }
+__device__ __forceinline__ float shfl_upv(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ double shfl_upv(double v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ DF shfl_upv(DF v) { return DF(shfl_upv(v.hi), shfl_upv(v.lo)); }
 
 // warps per CTA: 16 in FP32 (15 owned node rows), 8 in FP64 (shared memory and registers)
 template <class T>
@@ -72,17 +92,17 @@ constexpr unsigned FULL = 0xffffffffu;
 template <class T>
 __device__ __forceinline__ V3<T> shfl_down3(const V3<T>& v) {
     V3<T> r;
-    r.xy.x = __shfl_down_sync(FULL, v.xy.x, 1);
-    r.xy.y = __shfl_down_sync(FULL, v.xy.y, 1);
-    r.z = __shfl_down_sync(FULL, v.z, 1);
+    r.xy.x = shfl_dn(v.xy.x);
+    r.xy.y = shfl_dn(v.xy.y);
+    r.z = shfl_dn(v.z);
     return r;
 }
 template <class T>
 __device__ __forceinline__ V3<T> shfl_up3(const V3<T>& v) {
     V3<T> r;
-    r.xy.x = __shfl_up_sync(FULL, v.xy.x, 1);
-    r.xy.y = __shfl_up_sync(FULL, v.xy.y, 1);
-    r.z = __shfl_up_sync(FULL, v.z, 1);
+    r.xy.x = shfl_upv(v.xy.x);
+    r.xy.y = shfl_upv(v.xy.y);
+    r.z = shfl_upv(v.z);
     return r;
 }
 
@@ -254,7 +274,7 @@ struct KuTile {
             e.nm = __ldg(a.nmask + n);
             if (MODE == KU_RESID || MODE == KU_CHEB) {  // CHEB0 has b staged already
 #pragma unroll
-                for (int c = 0; c < 3; ++c) e.b[c] = __ldg(a.b + 3 * n + c);
+                for (int c = 0; c < 3; ++c) e.b[c] = ldg_t(a.b + 3 * n + c);
             }
             if (MODE == KU_CHEB) {
 #pragma unroll
@@ -354,9 +374,19 @@ struct KuTile {
                     if (MODE == KU_APPLY_DOT) dot.add(u[c], v);
                 }
             } else if (MODE == KU_RESID) {
-                T* yp = a.y + 3 * n;
+                if constexpr (std::is_same<T, DF>::value) {  // FP32 residual, ||r||^2 in FP64
+                    float* rp = reinterpret_cast<float*>(a.y) + 3 * n;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? b[c] - y[c] : T(0);
+                    for (int c = 0; c < 3; ++c) {
+                        const double rd = (nm >> c) & 1 ? b[c].value() - y[c].value() : 0.0;
+                        rp[c] = (float)rd;
+                        dot.add_sq(rd);
+                    }
+                } else {
+                    T* yp = a.y + 3 * n;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? b[c] - y[c] : T(0);
+                }
             } else if (Smem::CH) {
                 const float esum = in.sprev + ex;
                 const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
@@ -430,7 +460,7 @@ __global__ void __launch_bounds__(KmCfg<T>::NT, KmCfg<T>::MINB) ku_kernel(KuArgs
         cp_async_wait<0>();
         __syncthreads();  // the ring is idle before the next segment restages it
     }
-    if (MODE == KU_APPLY_DOT) {
+    if (MODE == KU_APPLY_DOT || (MODE == KU_RESID && std::is_same<T, DF>::value)) {
         const int tid = threadIdx.y * 32 + threadIdx.x;
         double v[1] = {dot.value()};
         block_sum<1, NT>(v, sred, tid);
@@ -465,6 +495,7 @@ void ku_prepare() {
     ku_resident<double, KU_RESID>();
     ku_resident<double, KU_CHEB>();
     ku_resident<double, KU_CHEB0>();
+    ku_resident<DF, KU_RESID>();
 }
 
 template <class T>
@@ -503,177 +534,34 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
     return ANL_OK;
 }
 
-// ------------------------------------------------------------------ accurate residual
-//
-// r = b - K x for x held in FP64 (as the pair x_hi + x_lo of floats), with K the operator of
-// the FP64 element blocks (each block entry a float pair hi + lo) and the FP32 element scales.
-// Differences, products and sums are carried as unevaluated float pairs (TwoSum / TwoProd),
-// so the result is accurate to about eps^2 of the summed terms: the FP32 CG certifies
-// ||b - K x|| <= rtol ||b|| for the FP64 operator, far below the FP32 rounding floor of a
-// plain evaluation (eps |K| |x|), at a fraction of the cost of FP64 arithmetic on this part.
-// The FP32 modal operator drives the recurrence; the periodic replacements by this residual
-// make the iteration converge to the FP64 operator's solution (iterative refinement).
-
-struct F2 {
-    float s, c;
-};
-
-__device__ __forceinline__ void f2_add(F2& a, float p) {
-    float t, e;
-    two_sum(a.s, p, t, e);
-    a.s = t;
-    a.c += e;
-}
-
-__global__ void __launch_bounds__(KU_NT, 1) ku_resid_hp_kernel(ResidHpArgs a, KeBlocks<float> kb,
-                                                                KeBlocks<float> kbl) {
-    __shared__ float sh[3][KU_HY][KU_HX][3];
-    __shared__ float sl[3][KU_HY][KU_HX][3];
-    __shared__ float sE[2][KU_EY][KU_EX];
-    __shared__ double sred[KU_NT / 32];
-    const Dims d = a.d;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * KU_BX + tx;
-    const int i0 = blockIdx.x * KU_BX, j0 = blockIdx.y * KU_BY, k0 = blockIdx.z * a.kz;
-    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-
-    auto load_nodes = [&](int slot, int kk) {
-        const bool kin = kk >= 0 && kk < NZn;
-        for (int f = tid; f < KU_HY * KU_HX * 3; f += KU_NT) {
-            const int row = f / (KU_HX * 3);
-            const int w = f - row * (KU_HX * 3);
-            const int c = w / 3, comp = w - 3 * c;
-            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
-            float vh = 0.f, vl = 0.f;
-            if (kin && gi >= 0 && gi < NXn && gj >= 0 && gj < NYn) {
-                const int64_t g = 3 * d.node(gi, gj, kk) + comp;
-                vh = a.xhi[g];
-                vl = a.xlo[g];
-            }
-            sh[slot][row][c][comp] = vh;
-            sl[slot][row][c][comp] = vl;
-        }
-    };
-    auto load_elems = [&](int slot, int ke) {
-        const bool kin = ke >= 0 && ke < d.nz;
-        for (int f = tid; f < KU_EY * KU_EX; f += KU_NT) {
-            const int row = f / KU_EX, c = f - row * KU_EX;
-            const int gi = i0 - 1 + c, gj = j0 - 1 + row;
-            float v = 0.f;
-            if (kin && gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny) v = a.E[d.elem(gi, gj, ke)];
-            sE[slot][row][c] = v;
-        }
-    };
-
-    load_nodes(0, k0 - 1);
-    load_nodes(1, k0);
-    load_elems(0, k0 - 1);
-    double rr = 0.0;
-    const int i = i0 + tx, j = j0 + ty;
-    const int kend = min(k0 + a.kz, NZn);
-    for (int k = k0; k < kend; ++k) {
-        const int r = k - k0;
-        const int sl3[3] = {r % 3, (r + 1) % 3, (r + 2) % 3};
-        const int e_lo = r & 1, e_hi = (r + 1) & 1;
-        load_nodes(sl3[2], k + 1);
-        load_elems(e_hi, k);
-        __syncthreads();
-        if (i < NXn && j < NYn) {
-            float uh[3], ul[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                uh[c] = sh[sl3[1]][ty + 1][tx + 1][c];
-                ul[c] = sl[sl3[1]][ty + 1][tx + 1][c];
-            }
-            F2 y[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll 1
-            for (int oct = 0; oct < 8; ++oct) {
-                const int sx = (oct & 1) ? 1 : -1, sy = (oct & 2) ? 1 : -1, sz = (oct & 4) ? 1 : -1;
-                const float Eo = sE[sz > 0 ? e_hi : e_lo][ty + (sy > 0 ? 1 : 0)][tx + (sx > 0 ? 1 : 0)];
-                if (Eo == 0.f) continue;
-                F2 w[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll
-                for (int dlt = 1; dlt < 8; ++dlt) {
-                    const int mx = sx * (dlt & 1), my = sy * ((dlt >> 1) & 1), mz = sz * ((dlt >> 2) & 1);
-                    const int slot = sl3[mz + 1];
-                    float th[3], tc[3];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float sg = c == 0 ? (float)sx : (c == 1 ? (float)sy : (float)sz);
-                        float dh, de;
-                        two_sum(sh[slot][ty + 1 + my][tx + 1 + mx][c], -uh[c], dh, de);
-                        const float dl = sl[slot][ty + 1 + my][tx + 1 + mx][c] - ul[c];
-                        th[c] = sg * dh;
-                        tc[c] = sg * (de + dl);
-                    }
-                    const float* B = kb.blk[dlt];
-                    const float* Bl = kbl.blk[dlt];  // the FP64 blocks = B + Bl to ~eps^2
-#pragma unroll
-                    for (int rr3 = 0; rr3 < 3; ++rr3)
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            float p, e;
-                            two_prod(B[3 * rr3 + c], th[c], p, e);
-                            f2_add(w[rr3], p);
-                            w[rr3].c += e + B[3 * rr3 + c] * tc[c] + Bl[3 * rr3 + c] * th[c];
-                        }
-                }
-#pragma unroll
-                for (int rr3 = 0; rr3 < 3; ++rr3) {
-                    const float sg = rr3 == 0 ? (float)sx : (rr3 == 1 ? (float)sy : (float)sz);
-                    float p, e;
-                    two_prod(sg * Eo, w[rr3].s, p, e);
-                    f2_add(y[rr3], p);
-                    y[rr3].c += e + sg * Eo * w[rr3].c;
-                }
-            }
-            const int64_t n = d.node(i, j, k);
-            const uint8_t nm = a.nmask[n];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                double rc = 0.0;
-                if ((nm >> c) & 1) rc = a.b[3 * n + c] - ((double)y[c].s + (double)y[c].c);
-                a.r[3 * n + c] = (float)rc;
-                rr = fma(rc, rc, rr);
-            }
-        }
-        __syncthreads();
-    }
-    double v[1] = {rr};
-    block_sum<1, KU_NT>(v, sred, tid);
-    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    const int nb = gridDim.x * gridDim.y * gridDim.z;
-    __shared__ double res[1];
-    if (finish_reduction<1, KU_NT>(v, bid, nb, a.partials, a.counter, res, tid, sred)) {
-        if (tid == 0) *a.rr_out = res[0];
-    }
-}
-
-int launch_resid_hp(const ResidHpArgs& args, const KeBlocks<float>& kb, const KeBlocks<float>& kbl, cudaStream_t s) {
-    ResidHpArgs a = args;
+// r = b - K x in double-float arithmetic (the modal form with the FP64 constants): a.u holds
+// x as (hi, lo) float pairs, a.b the FP64 right-hand side (as DF*), a.y receives the FP32
+// residual (as DF*), ||r||^2 goes to a.red_out.
+int launch_ku_resid_df(const KuArgs<DF>& args, const KeModal<DF>& km, cudaStream_t s) {
+    KuArgs<DF> a = args;
     const Dims& d = a.d;
     const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
-    const int chunks = ceil_div(NZn, 16);
-    a.kz = ceil_div(NZn, chunks);
-    dim3 grid(ceil_div(NXn, KU_BX), ceil_div(NYn, KU_BY), ceil_div(NZn, a.kz));
-    if ((int64_t)grid.x * grid.y * grid.z > a.partial_capacity) {
-        set_error("accurate residual: %d blocks exceed the reduction scratch (%d)", grid.x * grid.y * grid.z,
-                  a.partial_capacity);
+    const int64_t total = (int64_t)ceil_div(NXn, KmCfg<DF>::OX) * ceil_div(NYn, KmCfg<DF>::OY) * NZn;
+    const int resident = ku_resident<DF, KU_RESID>();
+    a.kz = (int)std::max<int64_t>(2, (total + resident - 1) / resident);
+    const int blocks = (int)((total + a.kz - 1) / a.kz);
+    if (blocks > a.partial_capacity) {
+        set_error("accurate residual: %d blocks exceed the reduction scratch (%d)", blocks, a.partial_capacity);
         return ANL_ERR_BADARG;
     }
-    ku_resid_hp_kernel<<<grid, dim3(KU_BX, KU_BY), 0, s>>>(a, kb, kbl);
+    ku_kernel<DF, KU_RESID><<<blocks, dim3(32, KmCfg<DF>::NW), sizeof(KuSmem<DF, KU_RESID>), s>>>(a, km);
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }
 
-// Upper bound of the K u grids (one CTA per SM and resident slot, at most 8 per SM) and of
-// the residual grid (chunks of 16 planes): sizes the reduction scratch.
+// Upper bound of the K u grids (one CTA per SM and resident slot, at most 8 per SM): sizes the
+// reduction scratch.
 int ku_grid_blocks(const Dims& d) {
-    const int NXn = d.nx + 1, NYn = d.ny + 1, NZn = d.nz + 1;
+    (void)d;
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int bres = ceil_div(NXn, KU_BX) * ceil_div(NYn, KU_BY) * (ceil_div(NZn, 16) + 1);
-    return std::max(8 * sms, bres);
+    return 8 * sms;
 }
 
 template int launch_ku<float>(int, const KuArgs<float>&, const KeModal<float>&, cudaStream_t);

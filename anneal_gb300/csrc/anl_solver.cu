@@ -436,6 +436,12 @@ __global__ void k_split(int64_t n, const double* x, T* hi, T* lo) {
     }
 }
 
+// x (FP64) -> (hi, lo) float pairs
+__global__ void k_split_df(int64_t n, const double* x, DF* xdf) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        xdf[i] = DF(x[i]);
+}
+
 // r = b - y1 - y2 (y2 may be null), ||r||^2; sets the CG state from the true residual.
 template <class T>
 __global__ void k_true_resid(int64_t n, const double* b, const T* y1, const T* y2, T* r, PcgScalars* sc,
@@ -814,8 +820,10 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     return ANL_OK;
 }
 
-// r = b - K x with x in FP64 (ctx->xbuf): the FP64 operator in FP64 mode; in FP32 mode the
-// FP32 operator evaluated in float-pair arithmetic on x = hi + lo. Updates the CG state.
+// r = b - K x with x in FP64 (ctx->xbuf): the FP64 operator in FP64 mode. In FP32 mode either
+// the same FP64 operator in double-float arithmetic (accurate: certifies any rtol down to
+// about 1e-10) or the FP32 operator on x = hi + lo (plain: restarts the recurrence). Updates
+// the CG state.
 __global__ void k_resid_state(PcgScalars* sc, const double* rr, int set_state) {
     const double v = *rr;
     sc->rr_true = v;
@@ -842,11 +850,11 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s, bool accurat
         ANL_LAUNCH_CHECK();
         return ANL_OK;
     }
-    k_split<float><<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (float*)c->xhi, (float*)c->xlo);
-    ANL_LAUNCH_CHECK();
     if (!accurate) {
         // plain FP32 evaluation of K x_hi + K x_lo: enough to restart the recurrence, not to
         // certify convergence (its rounding floor is ~eps |K| |dx|)
+        k_split<float><<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (float*)c->xhi, (float*)c->xlo);
+        ANL_LAUNCH_CHECK();
         ANL_TRY(apply_level<T>(c, L0, (const T*)c->xhi, (T*)c->y1, s));
         ANL_TRY(apply_level<T>(c, L0, (const T*)c->xlo, (T*)c->y2, s));
         k_true_resid<T><<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (const T*)c->y1, (const T*)c->y2, r, c->sc, set_state,
@@ -854,19 +862,21 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s, bool accurat
         ANL_LAUNCH_CHECK();
         return ANL_OK;
     }
-    ResidHpArgs a;
+    // r = b - K x of the FP64 modal operator in double-float arithmetic (FP32 residual out)
+    k_split_df<<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (DF*)c->xdf);
+    ANL_LAUNCH_CHECK();
+    KuArgs<DF> a;
     a.d = L0.d;
     a.E = L0.E;
     a.nmask = L0.nmask;
-    a.xhi = (const float*)c->xhi;
-    a.xlo = (const float*)c->xlo;
-    a.b = c->bbuf;
-    a.r = (float*)(void*)r;
+    a.u = (const DF*)c->xdf;
+    a.b = (const DF*)(const void*)c->bbuf;
+    a.y = (DF*)(void*)r;
     a.partials = c->partials;
     a.counter = c->counter;
     a.partial_capacity = c->part_cap;
-    a.rr_out = c->red_out + 8;
-    ANL_TRY(launch_resid_hp(a, c->kbf, c->kbf_lo, s));
+    a.red_out = c->red_out + 8;
+    ANL_TRY(launch_ku_resid_df(a, c->kmdf, s));
     k_resid_state<<<1, 1, 0, s>>>(c->sc, c->red_out + 8, set_state);
     ANL_LAUNCH_CHECK();
     return ANL_OK;
@@ -998,7 +1008,7 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
         const bool want_check = h.done == 1 || h.done == 2 || h.done == 4 || h.iters - last_replace >= 50 ||
                                 (h.rr <= 1e-6 * rr_replace && h.rr > 100.0 * h.tol2);
         if (!want_check) continue;
-        // Every replacement takes the accurate residual of the FP64 element blocks. The FP32
+        // Every replacement takes the accurate residual of the FP64 operator. The FP32
         // operator differs from them by a few eps in every element force, which leaves a
         // residual of several rtol in high-frequency modes at the end of an FP32 recurrence.
         // Taking the accurate residual already at the mid-solve replacement lets the
