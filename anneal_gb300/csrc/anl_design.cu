@@ -45,16 +45,33 @@ struct FilterArgs {
     double* red_out;
 };
 
-__device__ __forceinline__ float oc_xn(float x, float dcx, float dvx, float lam, float move) {
-    // optimize.py:150-152: ratio = sqrt(max(-dcx,0) / max(dvx*lam, 1e-300)),
-    // xn = clip(x*ratio, max(0, x-mv), min(1, x+mv))
+// optimize.py:150-152: ratio = sqrt(max(-dcx,0) / max(dvx*lam, 1e-300)),
+// xn = clip(x*ratio, max(0, x-mv), min(1, x+mv)). Split into the part of an element that does
+// not depend on lambda (x sqrt(max(-dcx,0)/dvx)) and one multiply by 1/sqrt(lambda), so a bank
+// of lambdas costs a multiply and a clamp each.
+struct OcElem {
+    float s;       // x sqrt(max(-dcx, 0) / dvx)
+    float dvx;
+    float lo, hi;  // the move limits
+    bool grows;    // max(-dcx, 0) > 0 and x > 0: the ratio is huge where dvx lambda underflows
+};
+__device__ __forceinline__ OcElem oc_elem(float x, float dcx, float dvx, float move) {
+    OcElem o;
     const float num = fmaxf(-dcx, 0.f);
-    const float den = dvx * lam;
-    float v;
-    if (den > 1e-30f) v = x * sqrtf(num / den);
-    else v = (num > 0.f && x > 0.f) ? INFINITY : 0.f;  // the FP64 guard 1e-300 makes the ratio huge
-    const float lo = fmaxf(0.f, x - move), hi = fminf(1.f, x + move);
-    return fminf(fmaxf(v, lo), hi);
+    o.s = dvx > 0.f ? x * sqrtf(num / dvx) : 0.f;
+    o.dvx = dvx;
+    o.lo = fmaxf(0.f, x - move);
+    o.hi = fminf(1.f, x + move);
+    o.grows = num > 0.f && x > 0.f;
+    return o;
+}
+__device__ __forceinline__ float oc_rl(float lam) { return 1.f / sqrtf(lam); }
+__device__ __forceinline__ float oc_xn(const OcElem& o, float lam, float rl) {
+    const float v = o.dvx * lam > 1e-30f ? o.s * rl : (o.grows ? INFINITY : 0.f);
+    return fminf(fmaxf(v, o.lo), o.hi);
+}
+__device__ __forceinline__ float oc_xn(float x, float dcx, float dvx, float lam, float move) {
+    return oc_xn(oc_elem(x, dcx, dvx, move), lam, oc_rl(lam));
 }
 
 template <int MODE>
@@ -433,13 +450,17 @@ __global__ void k_oc_vol_bank(int64_t ne, const uint8_t* active, const uint8_t* 
                               double* partials, unsigned* counter, double* out) {
     __shared__ double sm[OC_BANK * DT / 32];
     Acc2 acc[OC_BANK];
+    float rl[OC_BANK];
+#pragma unroll
+    for (int j = 0; j < OC_BANK; ++j) rl[j] = oc_rl(bank.lam[j]);
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
         if (active[e]) {
             const bool fz = frozen[e] != 0;
-            const float xe = x[e], ce = dcx[e], ve = dvx[e], we = wv[e];
+            const OcElem o = oc_elem(x[e], dcx[e], dvx[e], move);
+            const float we = wv[e];
 #pragma unroll
             for (int j = 0; j < OC_BANK; ++j)
-                if (j < bank.n) acc[j].add_prod(we, fz ? 1.f : oc_xn(xe, ce, ve, bank.lam[j], move));
+                if (j < bank.n) acc[j].add_prod(we, fz ? 1.f : oc_xn(o, bank.lam[j], rl[j]));
         }
     double v[OC_BANK];
 #pragma unroll
