@@ -233,6 +233,7 @@ static void free_ctx(anl_ctx* c) {
     f(c->q);
     f(c->xhi);
     f(c->xdf);
+    f(c->bdf);
     f(c->xlo);
     f(c->y1);
     f(c->y2);
@@ -363,7 +364,10 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     ALLOC(c->q, 3 * nn * ts);
     ALLOC(c->xhi, 3 * nn * ts);
     ALLOC(c->xlo, 3 * nn * ts);
-    if (!c->fp64) ALLOC(c->xdf, 3 * nn * sizeof(DF));
+    if (!c->fp64) {
+        ALLOC(c->xdf, 3 * nn * sizeof(DF));
+        ALLOC(c->bdf, 3 * nn * sizeof(DF));
+    }
     ALLOC(c->y1, 3 * nn * ts);
     ALLOC(c->y2, 3 * nn * ts);
     ALLOC(c->tmp, 3 * nn * ts);

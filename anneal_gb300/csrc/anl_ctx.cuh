@@ -82,6 +82,7 @@ struct anl_ctx {
     void* xhi = nullptr;
     void* xlo = nullptr;
     void* xdf = nullptr;  // FP32 mode: x as (hi, lo) float pairs for the accurate residual
+    void* bdf = nullptr;  // FP32 mode: the right-hand side as (hi, lo) float pairs
     void* y1 = nullptr;
     void* y2 = nullptr;
     void* tmp = nullptr;

@@ -57,18 +57,20 @@ struct DotAcc<double> {
     __device__ double value() const { return s; }
 };
 template <>
-struct DotAcc<DF> {  // the accurate residual: ||r||^2 in FP64
-    double s = 0.0;
-    __device__ void add(DF x, DF y) { s = fma(x.value(), y.value(), s); }
-    __device__ void add_sq(double v) { s = fma(v, v, s); }
-    __device__ double value() const { return s; }
+struct DotAcc<DF> {  // the accurate residual: ||r||^2 of its FP32 values, compensated
+    Acc2 a;
+    __device__ void add(DF x, DF y) { a.add_prod(x.hi + x.lo, y.hi + y.lo); }
+    __device__ void add_sq(float v) { a.add_prod(v, v); }
+    __device__ double value() const { return a.value(); }
 };
 
-// node-field loads of the epilogue; the double-float residual reads its right-hand side from
-// an FP64 vector and splits it
+// node-field loads of the epilogue
 __device__ __forceinline__ float ldg_t(const float* p) { return __ldg(p); }
 __device__ __forceinline__ double ldg_t(const double* p) { return __ldg(p); }
-__device__ __forceinline__ DF ldg_t(const DF* p) { return DF(__ldg(reinterpret_cast<const double*>(p))); }
+__device__ __forceinline__ DF ldg_t(const DF* p) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    return DF(t.x, t.y);
+}
 
 __device__ __forceinline__ float shfl_dn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 __device__ __forceinline__ double shfl_dn(double v) { return __shfl_down_sync(0xffffffffu, v, 1); }
@@ -374,13 +376,14 @@ struct KuTile {
                     if (MODE == KU_APPLY_DOT) dot.add(u[c], v);
                 }
             } else if (MODE == KU_RESID) {
-                if constexpr (std::is_same<T, DF>::value) {  // FP32 residual, ||r||^2 in FP64
+                if constexpr (std::is_same<T, DF>::value) {  // FP32 residual and ||r||^2
                     float* rp = reinterpret_cast<float*>(a.y) + 3 * n;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const double rd = (nm >> c) & 1 ? b[c].value() - y[c].value() : 0.0;
-                        rp[c] = (float)rd;
-                        dot.add_sq(rd);
+                        const DF rd = b[c] - y[c];
+                        const float rf = (nm >> c) & 1 ? rd.hi + rd.lo : 0.f;
+                        rp[c] = rf;
+                        dot.add_sq(rf);
                     }
                 } else {
                     T* yp = a.y + 3 * n;
@@ -534,9 +537,9 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
     return ANL_OK;
 }
 
-// r = b - K x in double-float arithmetic (the modal form with the FP64 constants): a.u holds
-// x as (hi, lo) float pairs, a.b the FP64 right-hand side (as DF*), a.y receives the FP32
-// residual (as DF*), ||r||^2 goes to a.red_out.
+// r = b - K x in double-float arithmetic (the modal form with the FP64 constants): a.u and a.b
+// hold x and the right-hand side as (hi, lo) float pairs, a.y receives the FP32 residual (as
+// DF*), ||r||^2 goes to a.red_out.
 int launch_ku_resid_df(const KuArgs<DF>& args, const KeModal<DF>& km, cudaStream_t s) {
     KuArgs<DF> a = args;
     const Dims& d = a.d;

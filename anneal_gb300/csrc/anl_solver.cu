@@ -870,7 +870,7 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s, bool accurat
     a.E = L0.E;
     a.nmask = L0.nmask;
     a.u = (const DF*)c->xdf;
-    a.b = (const DF*)(const void*)c->bbuf;
+    a.b = (const DF*)c->bdf;
     a.y = (DF*)(void*)r;
     a.partials = c->partials;
     a.counter = c->counter;
@@ -953,6 +953,10 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
     ANL_LAUNCH_CHECK();
     k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, x, L0.nmask, c->xbuf);
     ANL_LAUNCH_CHECK();
+    if (sizeof(T) == 4) {  // the right-hand side of the accurate residual, split once per solve
+        k_split_df<<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (DF*)c->bdf);
+        ANL_LAUNCH_CHECK();
+    }
     k_dot_d<<<vgrid(n), VT, 0, s>>>(n, c->bbuf, c->bbuf, c->partials, c->counter, c->red_out);
     ANL_LAUNCH_CHECK();
     k_init_scalars<<<1, 1, 0, s>>>(c->sc, rtol, maxiter, c->red_out);
