@@ -384,6 +384,78 @@ __global__ void __launch_bounds__(128) k_chol_inverse(const double* L, double* A
     for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i];
 }
 
+// The same factorisation and inverse with the matrix in shared memory, for n <= kCholSmemN
+// (n^2 doubles within the 227 KB a CTA may hold): no global round trip per column step, and
+// the inverse multiplies by precomputed reciprocal pivots.
+constexpr int kCholSmemN = 160;
+
+__global__ void __launch_bounds__(1024) k_cholesky_smem(double* A, int n, int* flag) {
+    extern __shared__ double S[];
+    __shared__ double piv, dmax;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) S[t] = A[t];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int j = 0; j < n; ++j) m = fmax(m, S[j * n + j]);
+        dmax = m;
+    }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        if (threadIdx.x == 0) {
+            const double a = S[j * n + j];
+            // tiny pivots are regularised as in k_cholesky
+            if (!(a > 1e-12 * dmax)) {
+                *flag += 1;
+                piv = sqrt(1e-12 * dmax);
+            } else {
+                piv = sqrt(a);
+            }
+            S[j * n + j] = piv;
+        }
+        __syncthreads();
+        const double rp = 1.0 / piv;
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) S[i * n + j] *= rp;
+        __syncthreads();
+        // trailing update of the lower triangle: one thread per (i, k), k <= i
+        const int m = n - j - 1;
+        for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+            const int i = j + 1 + t / m, k = j + 1 + t % m;
+            if (k <= i) S[i * n + k] -= S[i * n + j] * S[k * n + j];
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) A[t] = S[t];
+}
+
+__global__ void __launch_bounds__(256) k_chol_inverse_smem(const double* L, double* Ainv, int n) {
+    extern __shared__ double S[];  // L (n * n), reciprocal pivots (n), the column (n)
+    double* rd = S + n * n;
+    double* xs = rd + n;
+    const int c = blockIdx.x;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) S[t] = L[t];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        rd[i] = 1.0 / S[i * n + i];
+        xs[i] = i == c ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int j = c; j < n; ++j) {  // L y = e_c (y_j = 0 for j < c)
+        const double yj = xs[j] * rd[j];
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) xs[i] -= S[i * n + j] * yj;
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = yj;
+        __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {  // L^T x = y
+        const double xj = xs[j] * rd[j];
+        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] -= S[j * n + i] * xj;
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = xj;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i];
+}
+
 // x = A^-1 b on the coarsest grid (FP64), one warp per row.
 template <class T>
 __global__ void k_coarse_apply(const double* Ainv, int n, const T* b, const uint8_t* nmask, T* x, const int* done) {
@@ -720,10 +792,26 @@ static int coarse_factor(anl_ctx* c, cudaStream_t s) {
     k_assemble_dense<<<(int)std::min<int64_t>(4096, (total + 255) / 256), 256, 0, s>>>(L.d, L.E, L.nmask, c->ke_d, n, c->A);
     ANL_LAUNCH_CHECK();
     ANL_CUDA(cudaMemsetAsync(c->flag_d, 0, sizeof(int), s));
-    k_cholesky<<<1, 1024, 0, s>>>(c->A, n, c->flag_d);
-    ANL_LAUNCH_CHECK();
-    k_chol_inverse<<<n, 128, n * sizeof(double), s>>>(c->A, c->Ainv, n);
-    ANL_LAUNCH_CHECK();
+    if (n <= kCholSmemN) {
+        const int fb = n * n * (int)sizeof(double), ib = (n * n + 2 * n) * (int)sizeof(double);
+        static bool attr = false;
+        if (!attr) {
+            ANL_CUDA(cudaFuncSetAttribute(k_cholesky_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kCholSmemN * kCholSmemN * (int)sizeof(double)));
+            ANL_CUDA(cudaFuncSetAttribute(k_chol_inverse_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (kCholSmemN * kCholSmemN + 2 * kCholSmemN) * (int)sizeof(double)));
+            attr = true;
+        }
+        k_cholesky_smem<<<1, 1024, fb, s>>>(c->A, n, c->flag_d);
+        ANL_LAUNCH_CHECK();
+        k_chol_inverse_smem<<<n, 256, ib, s>>>(c->A, c->Ainv, n);
+        ANL_LAUNCH_CHECK();
+    } else {
+        k_cholesky<<<1, 1024, 0, s>>>(c->A, n, c->flag_d);
+        ANL_LAUNCH_CHECK();
+        k_chol_inverse<<<n, 128, n * sizeof(double), s>>>(c->A, c->Ainv, n);
+        ANL_LAUNCH_CHECK();
+    }
     c->coarse_ready = true;
     return ANL_OK;
 }
