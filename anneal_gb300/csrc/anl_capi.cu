@@ -194,13 +194,13 @@ int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* m
 
 // ------------------------------------------------------------------ context
 
-// the smoother's coefficients for every level (the last one, when it is not solved densely,
-// gets a 16-step sweep)
+// the smoother's coefficients for every level: kChebMax steps (the pair of step k does not
+// depend on how many steps a sweep takes, so every level reads the prefix it needs: 2 steps on
+// levels 0-1, mg_degree_coarse below, 16 on a last level that is not solved densely)
 static cudaError_t upload_cheb(anl_ctx* c) {
     std::vector<double> h(c->lev.size() * kChebStride, 0.0);
     for (size_t l = 0; l < c->lev.size(); ++l) {
-        const bool last = l + 1 == c->lev.size();
-        cheb_coefficients(c->lmax_bound, last ? 16 : c->mg_degree, h.data() + l * kChebStride);
+        cheb_coefficients(c->lmax_bound, kChebMax, h.data() + l * kChebStride);
         c->lev[l].lmax = c->lmax_bound;
     }
     return cudaMemcpy(c->cheb_d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);

@@ -892,7 +892,8 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
         return smooth<T>(c, L, 16, true, done, s);
     }
     Level& C = c->lev[l + 1];
-    ANL_TRY(smooth<T>(c, L, c->mg_degree, true, done, s));
+    const int deg = l >= 2 ? c->mg_degree_coarse : c->mg_degree;
+    ANL_TRY(smooth<T>(c, L, deg, true, done, s));
     KuArgs<T> a = ku_args<T>(c, L);
     a.u = (const T*)L.x;
     a.b = (const T*)L.b;
@@ -904,7 +905,7 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     ANL_TRY(vcycle<T>(c, l + 1, done, s));
     k_prolong_add<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
     ANL_LAUNCH_CHECK();
-    ANL_TRY(smooth<T>(c, L, c->mg_degree, false, done, s));
+    ANL_TRY(smooth<T>(c, L, deg, false, done, s));
     return ANL_OK;
 }
 
