@@ -165,7 +165,7 @@ double ke_modal(const double* ke, KeModal<double>* out) {
 
 // ------------------------------------------------------------------ declarations from other units
 
-void cheb_coefficients(double bound, int degree, double* out);
+void cheb_coefficients(double bound, double lo_frac, int degree, double* out);
 
 int solver_setup_domain(anl_ctx* c, const uint8_t* active, const uint8_t* fixed, cudaStream_t s);
 int solver_apply(anl_ctx* c, const float* escale, const void* u, void* y, cudaStream_t s);
@@ -200,7 +200,7 @@ int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* m
 static cudaError_t upload_cheb(anl_ctx* c) {
     std::vector<double> h(c->lev.size() * kChebStride, 0.0);
     for (size_t l = 0; l < c->lev.size(); ++l) {
-        cheb_coefficients(c->lmax_bound, kChebMax, h.data() + l * kChebStride);
+        cheb_coefficients(c->lmax_bound, l >= 2 ? c->cheb_lo_coarse : c->cheb_lo, kChebMax, h.data() + l * kChebStride);
         c->lev[l].lmax = c->lmax_bound;
     }
     return cudaMemcpy(c->cheb_d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);

@@ -65,10 +65,23 @@ struct anl_ctx {
 #endif
     int mg_degree = ANL_MG_DEGREE;
     // Levels 2 and below: their launches cost about the same whatever their size (launch and
-    // pipeline-fill latency), so more smoothing there is nearly free and saves CG iterations.
-    // Measured on the 256x128x128 L-bracket (CG iterations per solve, SIMP iterations/s):
-    // degree 2: 48.3, 21.4; 3: 41.2, 23.5; 4: 36.2, 25.2; 6: 32.6, 25.3; 8: 30.6, 24.8.
-    int mg_degree_coarse = 6;
+    // pipeline-fill latency), so more and deeper smoothing there is nearly free and saves CG
+    // iterations. Measured on the 256x128x128 L-bracket (interval low ends fine / coarse,
+    // coarse degree: CG iterations per solve, SIMP iterations/s):
+    //   0.05 / 0.05, 2: 48.3, 21.4     0.05 / 0.05, 6: 32.6, 25.3    0.03 / 0.01, 6: 28.8, 28.2
+    //   0.03 / 0.002, 6: 27.7, 29.2    0.03 / 0.002, 8: 24.1, 30.4   0.03 / 0.0005, 8: 24.5, 30.0
+#ifndef ANL_MG_DEGREE_COARSE
+#define ANL_MG_DEGREE_COARSE 8
+#endif
+    int mg_degree_coarse = ANL_MG_DEGREE_COARSE;
+#ifndef ANL_CHEB_LO
+#define ANL_CHEB_LO 0.03
+#endif
+#ifndef ANL_CHEB_LO_COARSE
+#define ANL_CHEB_LO_COARSE 0.002
+#endif
+    // lower ends of the smoothed intervals, as fractions of their upper end (levels 0-1, 2+)
+    double cheb_lo = ANL_CHEB_LO, cheb_lo_coarse = ANL_CHEB_LO_COARSE;
     // per level: {lambda_max bound, then (c1, c2) for up to kChebMax steps}, read by the
     // smoothing kernels from device memory
     double* cheb_d = nullptr;

@@ -5,14 +5,15 @@
 //  * the operator is the matrix-free K u of anl_ku.cu (FP32, or FP64 with ANL_FLAG_FP64);
 //  * the preconditioner is a V-cycle on the voxel hierarchy (element dims halved per level):
 //    coarse element scale = (sum of the 8 children)/4 (their mean at Ke(2h) = 2 Ke(h)),
-//    trilinear prolongation P and restriction P^T, Chebyshev smoothing on D^-1 K over
-//    [0.05, 1] x the element bound lambda_max(Ke) / Ke_00 (an upper bound of the spectrum for
-//    every design), and a dense FP64 Cholesky solve on the coarsest grid, refactored every
-//    solve (a high-degree Chebyshev sweep if that grid is too large for a dense factor);
+//    trilinear prolongation P and restriction P^T, Chebyshev smoothing on D^-1 K below the
+//    element bound lambda_max(Ke) / Ke_00 (an upper bound of the spectrum for every design):
+//    2 steps over [0.03, 1] x bound on levels 0-1, 8 steps over [0.002, 1] x bound on the
+//    latency-bound levels below; a dense FP64 Cholesky solve on the coarsest grid, refactored
+//    every solve (a high-degree Chebyshev sweep if that grid is too large for a dense factor);
 //  * the CG iterate x and right-hand side stay in FP64; the CG scalars come from FP64
-//    reductions (compensated FP32 partials); the residual is replaced by the true
-//    residual b - K x (x split as hi + lo in FP32) periodically and before convergence is
-//    accepted, so the stopping test ||b - K x|| <= rtol ||b|| holds for the true residual;
+//    reductions (compensated FP32 partials); the residual is replaced by the true residual
+//    b - K x of the FP64 operator (in double-float arithmetic) periodically and before
+//    convergence is accepted, so the stopping test ||b - K x|| <= rtol ||b|| holds for it;
 //  * beta is the flexible (Polak-Ribiere) form, robust to the FP32 preconditioner;
 //  * every loop kernel checks a device "done" flag, so the host enqueues a few iterations
 //    at a time and synchronises once per chunk.
@@ -761,17 +762,13 @@ static int apply_level(anl_ctx* c, const Level& L, const T* u, T* y, cudaStream_
 
 static int level_index(const anl_ctx* c, const Level& L) { return (int)(&L - &c->lev[0]); }
 
-#ifndef ANL_CHEB_LO
-#define ANL_CHEB_LO 0.05  // lower end of the smoothed interval, as a fraction of its upper end
-#endif
-
-// Chebyshev coefficients of a `degree`-step sweep of D^-1 K over [ANL_CHEB_LO, 1] x bound,
+// Chebyshev coefficients of a `degree`-step sweep of D^-1 K over [lo_frac, 1] x bound,
 // where bound = lambda_max(Ke) / Ke_00 >= lambda_max(D^-1 K) on every level and for every
 // design: out = {bound, c1_0, c2_0, c1_1, c2_1, ...}. A power-iteration estimate of the
 // spectrum approaches lambda_max from below and misses the localised top modes of solid
 // voxels inside void, which a sweep above its interval amplifies; the bound cannot.
-void cheb_coefficients(double bound, int degree, double* out) {
-    const double hi = bound, lo = ANL_CHEB_LO * bound;
+void cheb_coefficients(double bound, double lo_frac, int degree, double* out) {
+    const double hi = bound, lo = lo_frac * bound;
     const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
     double rho_old = 1.0 / sigma;
     out[0] = bound;
