@@ -13,7 +13,6 @@
 #include <cstdio>
 #include <algorithm>
 #include <mutex>
-#include <utility>
 
 #include "../../include/anneal_gb300.h"
 
@@ -57,31 +56,6 @@ void set_error(const char* fmt, ...);
 std::recursive_mutex& device_sync_mutex();
 void count_launch();
 void count_launches(long long n);  // kernels replayed by a CUDA graph
-
-// Programmatic dependent launch: the multigrid chain (K u passes, transfers, coarse solve)
-// is launched with programmatic stream serialisation, so the next kernel's CTAs are placed on
-// idle SMs while the current one drains. Every kernel launched this way calls pdl_wait()
-// before it touches memory (the wait returns once the previous grid has completed and its
-// writes are visible) and pdl_trigger() to let its successor be scheduled early.
-#ifdef __CUDACC__
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
-template <typename... KArgs, typename... Args>
-inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                              Args&&... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
-#endif
 
 // Grows a device buffer to at least `need` elements of `elem` bytes (contents are not kept).
 template <class P>

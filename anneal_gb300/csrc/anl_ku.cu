@@ -422,8 +422,6 @@ __global__ void __launch_bounds__(KmCfg<T>::NT, KmCfg<T>::MINB) ku_kernel(KuArgs
     extern __shared__ __align__(16) unsigned char ku_smem_raw[];
     auto& sm = *reinterpret_cast<typename Tile::Smem*>(ku_smem_raw);
     __shared__ double sred[NT / 32];
-    pdl_wait();
-    pdl_trigger();
     if (a.done != nullptr && *a.done) return;
 
     Tile t(a, km, sm);
@@ -528,13 +526,11 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
         return ANL_ERR_BADARG;
     }
     switch (mode) {
-        case KU_APPLY: ANL_CUDA(launch_pdl(ku_kernel<T, KU_APPLY>, dim3(blocks), block, sizeof(KuSmem<T, KU_APPLY>), s, a, km)); break;
-        case KU_APPLY_DOT:
-            ANL_CUDA(launch_pdl(ku_kernel<T, KU_APPLY_DOT>, dim3(blocks), block, sizeof(KuSmem<T, KU_APPLY_DOT>), s, a, km));
-            break;
-        case KU_RESID: ANL_CUDA(launch_pdl(ku_kernel<T, KU_RESID>, dim3(blocks), block, sizeof(KuSmem<T, KU_RESID>), s, a, km)); break;
-        case KU_CHEB: ANL_CUDA(launch_pdl(ku_kernel<T, KU_CHEB>, dim3(blocks), block, sizeof(KuSmem<T, KU_CHEB>), s, a, km)); break;
-        case KU_CHEB0: ANL_CUDA(launch_pdl(ku_kernel<T, KU_CHEB0>, dim3(blocks), block, sizeof(KuSmem<T, KU_CHEB0>), s, a, km)); break;
+        case KU_APPLY: ku_kernel<T, KU_APPLY><<<blocks, block, sizeof(KuSmem<T, KU_APPLY>), s>>>(a, km); break;
+        case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<blocks, block, sizeof(KuSmem<T, KU_APPLY_DOT>), s>>>(a, km); break;
+        case KU_RESID: ku_kernel<T, KU_RESID><<<blocks, block, sizeof(KuSmem<T, KU_RESID>), s>>>(a, km); break;
+        case KU_CHEB: ku_kernel<T, KU_CHEB><<<blocks, block, sizeof(KuSmem<T, KU_CHEB>), s>>>(a, km); break;
+        case KU_CHEB0: ku_kernel<T, KU_CHEB0><<<blocks, block, sizeof(KuSmem<T, KU_CHEB0>), s>>>(a, km); break;
         default: return ANL_ERR_BADARG;
     }
     ANL_LAUNCH_CHECK();

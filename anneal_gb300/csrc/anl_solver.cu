@@ -169,8 +169,6 @@ template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const T* __restrict__ rf,
                                                           const uint8_t* __restrict__ nmc, T* __restrict__ bc,
                                                           const int* done) {
-    pdl_wait();
-    pdl_trigger();
     if (done && *done) return;
     const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y, K = blockIdx.z;
     if (I > c.nx || J > c.ny) return;
@@ -215,8 +213,6 @@ template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
                                                                 const uint8_t* __restrict__ nmf, T* __restrict__ xf,
                                                                 const int* done) {
-    pdl_wait();
-    pdl_trigger();
     if (done && *done) return;
     const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y, K = blockIdx.z;
     if (I > c.nx || J > c.ny) return;
@@ -464,8 +460,6 @@ __global__ void __launch_bounds__(256) k_chol_inverse_smem(const double* L, doub
 // x = A^-1 b on the coarsest grid (FP64), one warp per row.
 template <class T>
 __global__ void k_coarse_apply(const double* Ainv, int n, const T* b, const uint8_t* nmask, T* x, const int* done) {
-    pdl_wait();
-    pdl_trigger();
     if (done && *done) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -887,8 +881,8 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     if (l + 1 == c->lev.size()) {
         if (c->dense_coarse) {
             const int n = c->nc;
-            ANL_CUDA(launch_pdl(k_coarse_apply<T>, dim3(std::max(1, (n * 32 + 255) / 256)), dim3(256), 0, s,
-                                (const double*)c->Ainv, n, (const T*)L.b, (const uint8_t*)L.nmask, (T*)L.x, done));
+            k_coarse_apply<T><<<std::max(1, (n * 32 + 255) / 256), 256, 0, s>>>(c->Ainv, n, (const T*)L.b, L.nmask,
+                                                                             (T*)L.x, done);
             ANL_LAUNCH_CHECK();
             return ANL_OK;
         }
@@ -903,12 +897,10 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     a.y = (T*)L.r;
     a.done = done;
     ANL_TRY(launch_ku<T>(KU_RESID, a, modal_of<T>(c), s));
-    ANL_CUDA(launch_pdl(k_restrict<T>, transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s, L.d, C.d, (const T*)L.r,
-                        (const uint8_t*)C.nmask, (T*)C.b, done));
+    k_restrict<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<T>(c, l + 1, done, s));
-    ANL_CUDA(launch_pdl(k_prolong_add<T>, transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s, L.d, C.d, (const T*)C.x,
-                        (const uint8_t*)L.nmask, (T*)L.x, done));
+    k_prolong_add<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(smooth<T>(c, L, deg, false, done, s));
     return ANL_OK;
