@@ -9,7 +9,7 @@ energy-optimal combination of the previous iterate and the prediction:
 
 This minimises the initial energy-norm error over the two directions, so the start is never
 worse than the previous iterate in that norm, and a useless prediction gets b ~ 0. The CG
-still runs to the same relative residual and stays the judge of convergence.
+still runs to the same relative residual and alone decides convergence.
 
 Network (the learned-warm-start configuration): 4 levels, base channels doubling per level,
 two 3x3x3 convolutions with GELU per level, 2x average pooling down, 2x nearest upsampling

@@ -43,13 +43,13 @@ def run_loop(work, iters, warm=None):
             comp.append(rec["compliance"][0])
         dropped = warm is not None and run.warm_start is None
         gains = list(run.ws_gain)
-        judge = [(round(a_, 5), round(b_, 5)) for a_, b_ in run.ws_judge]
+        ledger = [(round(a_, 5), round(b_, 5)) for a_, b_ in run.ws_ledger]
         run.close()
     finally:
         OPT.EMIN = old
     return {"ms": 1e3 * float(np.mean(times[1:])), "cg": float(np.mean(cg[1:])), "cg_list": cg,
             "compliance_last": comp[-1], "dropped": dropped, "gains": [round(g, 6) for g in gains],
-            "saved_s_vs_predict_s": judge}
+            "saved_s_vs_predict_s": ledger}
 
 
 def main():

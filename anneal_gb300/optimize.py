@@ -134,7 +134,7 @@ class SimpRunner:
         # combination stops lowering the energy of the previous iterate
         self.warm_start = warm_start
         self.ws_gain = []
-        self.ws_judge = []
+        self.ws_ledger = []
         if warm_start is not None:
             fx = torch.zeros(3 * grid.nnode, dtype=torch.uint8, device="cuda")
             fx[torch.as_tensor(np.asarray(fixed, np.int64), device="cuda")] = 1
@@ -163,7 +163,7 @@ class SimpRunner:
         t_solve = time.perf_counter()
         fem.solve_device(self.escale_t, self.F_t, self.U_t, rtol=self.rtol, maxiter=self.maxiter, rebuild=rebuild)
         if ws is not None:
-            self._judge_learned_start(ws, time.perf_counter() - t_solve)
+            self._assess_learned_start(ws, time.perf_counter() - t_solve)
         if rebuild:
             self.base_iters = fem.cg_iters[-1]
         nc = len(self.cases)
@@ -200,7 +200,7 @@ class SimpRunner:
     def _learned_start(self):
         """Replaces each case's start by the energy-optimal combination of the previous
         iterate and the network's prediction (anneal_gb300.learned.galerkin_start). Returns
-        what the judgement after the solve needs."""
+        what the assessment after the solve needs."""
         from . import learned as LW
         ctx = self.ctx
         free = self._ws_free.double()
@@ -217,7 +217,7 @@ class SimpRunner:
         torch.cuda.synchronize()
         return info, time.perf_counter() - t0
 
-    def _judge_learned_start(self, ws, t_solve):
+    def _assess_learned_start(self, ws, t_solve):
         """After the solve, Pi(u) = u.Ku/2 - F.u of the solution gives the initial energy
         errors of both starts (Pi(x) - Pi(u*) = |x - u*|_K^2 / 2). CG needs iterations in
         proportion to log(initial / final energy error), the final one being about
@@ -238,8 +238,8 @@ class SimpRunner:
             if e_new > e_fin:
                 would = it * np.log(e_prev / e_fin) / np.log(e_new / e_fin)
                 saved_s += max(0.0, would - it) * t_solve / (nc * it)
-        self.ws_judge.append((saved_s, t_pred))
-        recent = self.ws_judge[-2:]
+        self.ws_ledger.append((saved_s, t_pred))
+        recent = self.ws_ledger[-2:]
         if len(recent) == 2 and all(sv < tp for sv, tp in recent):
             self.warm_start = None
 
