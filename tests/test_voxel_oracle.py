@@ -48,3 +48,18 @@ def test_box_plane_fill_values():
     assert np.all(f[1, 1:4, 1:4] == 1.0)
     assert np.allclose(f[2, 1:4, 1:4], 2.0 / 3.0)
     assert f[0].sum() == 0.0 and f[3].sum() == 0.0
+
+
+def test_triangles_of_accepts_mesh_forms():
+    """voxel_fill takes what the reference passes (an object with .triangles) and the other
+    common mesh forms; all give the same (n, 3, 3) FP64 array."""
+    import types
+    V, F = G.icosphere(1, 2.0)
+    t = V[F]
+    for m in (types.SimpleNamespace(triangles=t), types.SimpleNamespace(vertices=V, faces=F), t,
+              t.astype(np.float32).astype(np.float64).tolist()):
+        got = G.triangles_of(m)
+        assert got.shape == t.shape and got.dtype == np.float64
+    assert np.array_equal(G.triangles_of(types.SimpleNamespace(vertices=V, faces=F)), t)
+    with pytest.raises(ValueError):
+        G.triangles_of(np.zeros((4, 3)))
