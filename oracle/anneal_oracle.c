@@ -267,7 +267,15 @@ static double dot(int64_t n, const double* a, const double* b) {
  * Coarse levels halve the element grid; coarse element scale = (sum of the 8 children)/4,
  * i.e. the children's mean at Ke(2h) = 2 Ke(h); transfer = trilinear interpolation and
  * its transpose; Chebyshev smoothing on D^-1 K; dense Cholesky on the coarsest level.
+ * The smoother follows the GPU solver's, so that a CPU timing scaled by the GPU's CG
+ * iteration count compares like with like: below the element bound lambda_max(Ke) / Ke_00
+ * (an upper bound of the spectrum of D^-1 K for every design), `degree` steps over
+ * [ORC_LO, 1] x bound on levels 0 and 1 and ORC_DEG_COARSE steps over [ORC_LO_COARSE, 1] x
+ * bound below.
  */
+#define ORC_LO 0.03
+#define ORC_LO_COARSE 0.002
+#define ORC_DEG_COARSE 8
 typedef struct {
     int nx, ny, nz;
     int64_t nn, ndof;
@@ -279,7 +287,6 @@ typedef struct {
     double* b;
     double* r;
     double* d;
-    double lmax;
     double* chol; /* coarsest only, ndof x ndof */
 } level_t;
 
@@ -288,6 +295,7 @@ typedef struct {
     level_t lev[16];
     const double* ke;
     int degree;
+    double bound; /* lambda_max(Ke) / Ke_00, slightly enlarged */
 } mg_t;
 
 static void level_alloc(level_t* L, int nx, int ny, int nz) {
@@ -446,23 +454,25 @@ static void apply_level(const mg_t* mg, const level_t* L, const double* u, doubl
     orc_apply_K(L->nx, L->ny, L->nz, mg->ke, L->E, L->dofmask, u, y);
 }
 
-/* largest eigenvalue of D^-1 K by power iteration (deterministic start vector) */
-static double est_lmax(const mg_t* mg, level_t* L, int iters) {
-    int64_t n = L->ndof;
-    double* v = L->r;
-    double* w = L->d;
-    for (int64_t i = 0; i < n; ++i) v[i] = L->dofmask[i] ? 1.0 + 0.1 * (double)((i * 7919) % 13) : 0.0;
-    double lam = 1.0;
-    for (int it = 0; it < iters; ++it) {
-        double nv = sqrt(dot(n, v, v));
-        if (nv == 0) return 1.0;
-        for (int64_t i = 0; i < n; ++i) v[i] /= nv;
-        apply_level(mg, L, v, w);
-        for (int64_t i = 0; i < n; ++i) w[i] /= L->dg[i];
-        lam = dot(n, v, w);
-        memcpy(v, w, sizeof(double) * n);
+/* lambda_max(Ke) / Ke_00 by power iteration on the 24 x 24 element matrix */
+static double element_bound(const double* ke) {
+    double v[24], w[24], lam = 0.0;
+    for (int i = 0; i < 24; ++i) v[i] = 1.0 + 0.01 * i * ((i % 3) + 1) * ((i & 1) ? -1.0 : 1.0);
+    for (int it = 0; it < 500; ++it) {
+        double nv = 0.0;
+        for (int i = 0; i < 24; ++i) nv += v[i] * v[i];
+        nv = sqrt(nv);
+        for (int i = 0; i < 24; ++i) v[i] /= nv;
+        for (int i = 0; i < 24; ++i) {
+            double t = 0.0;
+            for (int j = 0; j < 24; ++j) t += ke[24 * i + j] * v[j];
+            w[i] = t;
+        }
+        lam = 0.0;
+        for (int i = 0; i < 24; ++i) lam += v[i] * w[i];
+        memcpy(v, w, sizeof(v));
     }
-    return lam;
+    return 1.001 * lam / ke[0];
 }
 
 static int chol_factor(double* A, int n) {
@@ -516,10 +526,12 @@ static int coarse_setup(const mg_t* mg, level_t* L) {
     return chol_factor(L->chol, n);
 }
 
-/* Chebyshev smoothing of K x = b on [0.1, 1.1] * lmax, `degree` steps, from the given x. */
+/* Chebyshev smoothing of K x = b below the element bound, from the given x */
 static void chebyshev(const mg_t* mg, level_t* L, int x_is_zero) {
     int64_t n = L->ndof;
-    double hi = 1.1 * L->lmax, lo = 0.1 * L->lmax;
+    const int coarse = (L - mg->lev) >= 2;
+    const int degree = coarse ? ORC_DEG_COARSE : mg->degree;
+    double hi = mg->bound, lo = (coarse ? ORC_LO_COARSE : ORC_LO) * mg->bound;
     double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
     double rho_old = 1.0 / sigma;
     if (x_is_zero) memcpy(L->r, L->b, sizeof(double) * n);
@@ -531,7 +543,7 @@ static void chebyshev(const mg_t* mg, level_t* L, int x_is_zero) {
         L->d[i] = L->r[i] / L->dg[i] / theta;
         L->x[i] += L->d[i];
     }
-    for (int s = 1; s < mg->degree; ++s) {
+    for (int s = 1; s < degree; ++s) {
         apply_level(mg, L, L->x, L->r);
         double rho = 1.0 / (2 * sigma - rho_old);
         for (int64_t i = 0; i < n; ++i) {
@@ -603,7 +615,7 @@ int orc_pcg(int nx, int ny, int nz, const double* ke, const double* E, const uin
             orc_diag(C->nx, C->ny, C->nz, ke, C->E, C->dofmask, C->dg);
             mg.nlev++;
         }
-        for (int l = 0; l < mg.nlev - 1; ++l) mg.lev[l].lmax = est_lmax(&mg, &mg.lev[l], 12);
+        mg.bound = element_bound(ke);
         if (mg.nlev == 1 || coarse_setup(&mg, &mg.lev[mg.nlev - 1]) != 0) {
             if (mg.nlev > 1) status = 2;
             precond = 0;
