@@ -18,10 +18,11 @@ ANL_ERR_CUDA = 5
 ANL_ERR_SINGULAR = 6
 ANL_ERR_NOMEM = 7
 ANL_ERR_STATE = 8
+ANL_ERR_STAGNATION = 9
 ANL_FLAG_FP64 = 1
 
 STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "NONFINITE", 3: "BREAKDOWN", 4: "BADARG", 5: "CUDA",
-                6: "SINGULAR", 7: "NOMEM", 8: "STATE"}
+                6: "SINGULAR", 7: "NOMEM", 8: "STATE", 9: "STAGNATION"}
 
 # Every symbol include/anneal_gb300.h declares; tests check the library exports them all.
 EXPORTS = [

@@ -98,8 +98,9 @@ class Context:
 
     def solve(self, escale, F, X, rtol, maxiter=2000, rebuild=True):
         """F, X: (nrhs, ndof) float64; X holds the initial guesses. Returns (status, iters,
-        relres) without raising on MAXITER / NONFINITE / BREAKDOWN / SINGULAR (the caller
-        decides: each means the part is not properly supported or the solve failed)."""
+        relres) without raising on MAXITER / NONFINITE / BREAKDOWN / SINGULAR / STAGNATION
+        (the caller decides: the first four mean the part is not properly supported or the
+        solve failed; STAGNATION asks for the FP64 context to finish an FP32 solve)."""
         _chk(escale, _F32, self.ne, "escale")
         nrhs = F.shape[0] if F.dim() == 2 else 1
         _chk(F, _F64, nrhs * self.ndof, "F")
@@ -109,7 +110,7 @@ class Context:
         st = self.lib.anl_solve(self._h, _p(escale), _p(F), _p(X), nrhs, float(rtol), int(maxiter),
                                 1 if rebuild else 0, iters, relres, _stream())
         if st not in (N.ANL_OK, N.ANL_ERR_MAXITER, N.ANL_ERR_NONFINITE, N.ANL_ERR_BREAKDOWN,
-                      N.ANL_ERR_SINGULAR):
+                      N.ANL_ERR_SINGULAR, N.ANL_ERR_STAGNATION):
             N.check(st, "anl_solve")
         return st, list(iters), list(relres)
 

@@ -393,7 +393,9 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         return ANL_ERR_CUDA;
     }
     c->use_graph = std::getenv("ANL_NO_GRAPH") == nullptr;
+    if (const char* e = std::getenv("ANL_BOX_FROM")) c->box_from = std::atoi(e);
     ku_prepare();
+    kbox_prepare();
     if (cudaMallocHost((void**)&c->sc_h, sizeof(PcgScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->red_h, 16 * sizeof(double)) != cudaSuccess) {
         set_error("pinned host allocation failed");

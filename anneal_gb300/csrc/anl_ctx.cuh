@@ -74,6 +74,9 @@ struct anl_ctx {
 #define ANL_MG_DEGREE_COARSE 8
 #endif
     int mg_degree_coarse = ANL_MG_DEGREE_COARSE;
+    // first level smoothed by the box kernels (anl_kbox.cu; FP32 contexts): on the levels below
+    // 128 x 64 x 64 elements a z-marching K u launch is a chain of latencies
+    int box_from = 2;
 #ifndef ANL_CHEB_LO
 #define ANL_CHEB_LO 0.03
 #endif

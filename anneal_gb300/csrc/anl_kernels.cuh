@@ -40,5 +40,38 @@ template <class T>
 int launch_ku(int mode, const KuArgs<T>& a, const KeModal<T>& km, cudaStream_t s);
 int launch_ku_resid_df(const KuArgs<DF>& a, const KeModal<DF>& km, cudaStream_t s);
 
+// ------------------------------------------------------------------ small-grid smoother passes
+
+// The passes of the V-cycle on the coarse levels, one CTA per 8 x 8 x 8 element box
+// (anl_kbox.cu), FP32:
+//   KB_RESID  y = b - K u
+//   KB_CHEB   one Chebyshev step: d <- c1 d + c2 D^-1 (b - K u), xout = u + d
+//   KB_CHEB0  the first two steps from x = 0 (x1 = c2_0 D^-1 b formed while staging)
+//   KB_PCHEB  u <- u + P xc (the coarse-grid correction) formed while staging, then the first
+//             step of a sweep (c1 = 0)
+enum { KB_RESID = 0, KB_CHEB = 1, KB_CHEB0 = 2, KB_PCHEB = 3 };
+
+struct KbArgs {
+    Dims d;
+    const float* E = nullptr;        // element scale (already times h), full grid
+    const uint8_t* nmask = nullptr;  // node mask bits
+    const float* diag = nullptr;     // inverse diagonal of K per node (0 where unused)
+    const float* u = nullptr;        // iterate (KB_RESID, KB_CHEB, KB_PCHEB)
+    const float* b = nullptr;        // right-hand side
+    float* y = nullptr;              // KB_RESID: the residual
+    float* dv = nullptr;             // Chebyshev direction (read by KB_CHEB unless c1_zero; written if dv_keep)
+    float* xout = nullptr;           // the new iterate
+    const double* cheb = nullptr;    // {c1, c2} of the step (KB_CHEB0: of step 1)
+    const double* cheb0 = nullptr;   // KB_CHEB0: {c1_0, c2_0}
+    int c1_zero = 0;                 // KB_CHEB: first step of a sweep
+    int dv_keep = 1;                 // 0 on the last step of a sweep
+    Dims dc{};                       // KB_PCHEB: the coarse level and its correction
+    const float* xc = nullptr;
+    const int* done = nullptr;       // early-exit flag of the CG loop (may be null)
+};
+
+int launch_kbox(int mode, const KbArgs& a, const KeModal<float>& km, cudaStream_t s);
+void kbox_prepare();
+
 
 }  // namespace anl

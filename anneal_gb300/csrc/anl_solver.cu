@@ -876,6 +876,77 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
 }
 
 template <class T>
+static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s);
+
+// One V-cycle step on a level the box kernels (anl_kbox.cu) smooth: the pre-smoothing sweep
+// from x = 0 (its first two steps fused), the residual, the restriction, the coarser levels,
+// then the post-smoothing sweep whose first step also adds the coarse-grid correction.
+static int vcycle_box(anl_ctx* c, size_t l, int deg, const int* done, cudaStream_t s) {
+    Level& L = c->lev[l];
+    Level& C = c->lev[l + 1];
+    const double* cf = c->cheb_d + l * kChebStride + 1;  // (c1, c2) pairs
+    KbArgs base;
+    base.d = L.d;
+    base.E = L.E;
+    base.nmask = L.nmask;
+    base.diag = L.diag;
+    base.b = (const float*)L.b;
+    base.done = done;
+    int k0 = 0;
+    if (deg >= 2) {
+        KbArgs a = base;
+        a.cheb0 = cf;
+        a.cheb = cf + 2;
+        a.dv = (float*)L.dv;
+        a.xout = (float*)L.x;
+        a.dv_keep = deg > 2;
+        ANL_TRY(launch_kbox(KB_CHEB0, a, c->kmf, s));
+        k0 = 2;
+    } else {
+        k_cheb_first<float><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const float*)L.b, L.diag, L.nmask, cf + 1,
+                                                            (float*)L.x, (float*)L.dv, done);
+        ANL_LAUNCH_CHECK();
+        k0 = 1;
+    }
+    for (int k = k0; k < deg; ++k) {
+        KbArgs a = base;
+        a.u = (const float*)L.x;
+        a.dv = (float*)L.dv;
+        a.xout = (float*)L.xt;
+        a.cheb = cf + 2 * k;
+        a.dv_keep = k + 1 < deg;
+        ANL_TRY(launch_kbox(KB_CHEB, a, c->kmf, s));
+        std::swap(L.x, L.xt);
+    }
+    {
+        KbArgs a = base;
+        a.u = (const float*)L.x;
+        a.y = (float*)L.r;
+        ANL_TRY(launch_kbox(KB_RESID, a, c->kmf, s));
+    }
+    k_restrict<float><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const float*)L.r, C.nmask,
+                                                                     (float*)C.b, done);
+    ANL_LAUNCH_CHECK();
+    ANL_TRY(vcycle<float>(c, l + 1, done, s));
+    for (int k = 0; k < deg; ++k) {
+        KbArgs a = base;
+        a.u = (const float*)L.x;
+        a.dv = (float*)L.dv;
+        a.xout = (float*)L.xt;
+        a.cheb = cf + 2 * k;
+        a.c1_zero = k == 0;
+        a.dv_keep = k + 1 < deg;
+        if (k == 0) {
+            a.dc = C.d;
+            a.xc = (const float*)C.x;
+        }
+        ANL_TRY(launch_kbox(k == 0 ? KB_PCHEB : KB_CHEB, a, c->kmf, s));
+        std::swap(L.x, L.xt);
+    }
+    return ANL_OK;
+}
+
+template <class T>
 static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     Level& L = c->lev[l];
     if (l + 1 == c->lev.size()) {
@@ -890,6 +961,7 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     }
     Level& C = c->lev[l + 1];
     const int deg = l >= 2 ? c->mg_degree_coarse : c->mg_degree;
+    if (sizeof(T) == 4 && (int)l >= c->box_from) return vcycle_box(c, l, deg, done, s);
     ANL_TRY(smooth<T>(c, L, deg, true, done, s));
     KuArgs<T> a = ku_args<T>(c, L);
     a.u = (const T*)L.x;
@@ -1121,12 +1193,19 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
         }
         // At the attainable accuracy of the operator's arithmetic the true residual stops
         // falling while the recurrence keeps converging (the reference's scipy CG stops on
-        // the recurrence alone and never sees this floor). Accept once a further round of
-        // iterations has not halved the true residual, if it is within
-        // max(100 rtol, 1e-10) relative.
+        // the recurrence alone and never sees this floor). In FP64 a solve is accepted once
+        // a further round of iterations has not halved the true residual, if it is within
+        // max(100 rtol, 1e-10) relative (the reported relres then exceeds rtol). An FP32
+        // solve that stops falling above rtol returns ANL_ERR_STAGNATION instead, so the
+        // caller can finish it in FP64: FP32 results always meet rtol.
         const double floor2 = std::max(1e4 * t.tol2, 1e-20 * t.bb);
         if (h.done == 1 || h.done == 4) {
-            if (stag_ref > 0 && t.rr_true <= floor2 && t.rr_true >= 0.25 * stag_ref) break;
+            const bool stalled = stag_ref > 0 && t.rr_true >= 0.25 * stag_ref;
+            if (stalled && sizeof(T) == 4) {
+                status = ANL_ERR_STAGNATION;
+                break;
+            }
+            if (stalled && t.rr_true <= floor2) break;
             if (stag_ref < 0 || t.rr_true < stag_ref) stag_ref = t.rr_true;
             if (h.done == 4 && t.rr_true > floor2) {
                 status = ANL_ERR_BREAKDOWN;
@@ -1213,6 +1292,8 @@ int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, in
     if (worst == ANL_ERR_MAXITER) set_error("CG did not reach rtol %.3g in %d iterations", rtol, maxiter);
     if (worst == ANL_ERR_NONFINITE) set_error("a non-finite value appeared in CG");
     if (worst == ANL_ERR_BREAKDOWN) set_error("CG breakdown: the operator is not positive definite on the free DOFs");
+    if (worst == ANL_ERR_STAGNATION)
+        set_error("FP32 CG stopped improving above rtol %.3g (finish the solve in FP64)", rtol);
     return worst;
 }
 

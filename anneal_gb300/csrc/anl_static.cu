@@ -1,11 +1,13 @@
 // anl_static.cu -- the compliance dot product without any device allocation.
 //
 // Who needs this: callers that cannot call cudaMalloc at the point where they need the
-// compliance. Examples are code running inside a CUDA host callback or a memory-pool hook
-// (where allocating is not allowed), embedders whose framework owns the whole device memory
-// pool and hands out only the tensors it created, and real-time loops that must not risk an
-// allocation (or its implicit device synchronisation) in the middle of a step. They cannot create
-// an anl_ctx either, because anl_ctx_create allocates the solver workspaces.
+// compliance. Examples are a memory-pool hook or allocator callback (which must not
+// re-enter the allocator), embedders whose framework owns the whole device memory pool and
+// hands out only the tensors it created, and real-time loops that must not risk an
+// allocation (or its implicit device synchronisation) in the middle of a step. They cannot
+// create an anl_ctx either, because anl_ctx_create allocates the solver workspaces. (Code
+// inside a CUDA host function or stream callback may make no CUDA call at all, so it cannot
+// use this entry point either.)
 //
 // anl_dot_static gives them the same FP64 dot product as anl_dot (the compliance f . u of a
 // SIMP iteration) with caller-owned inputs and output. The reduction scratch (one partial
@@ -27,31 +29,27 @@ constexpr int kScratchWords = kStaticBlocks + 32;     // partials, then the tick
 
 // File-scope scratch shared by every call on a device: partials[0..kStaticBlocks) and the
 // ticket counter in word kStaticBlocks. Host code must not take its address directly (the
-// host-side name is only a stand-in); it asks the runtime for the device address once per
-// device (scratch_on_current_device).
+// host-side name is only a stand-in); every call asks the runtime for the device address in
+// the current device's context (cheap once the module is loaded, and never stale after a
+// device reset or under another context). The lookup holds the library's device lock, as
+// every call that may load a module or synchronise does, so it cannot invalidate a graph
+// capture running on another thread.
 static __device__ __align__(256) double g_static_scratch[kScratchWords];
 
-std::mutex g_mu;
-void* g_scratch_ptr[64] = {};
-
 int scratch_on_current_device(double** out) {
-    int dev = -1;
-    ANL_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) {
-        set_error("anl_dot_static: device ordinal %d is outside the supported range 0..63", dev);
-        return ANL_ERR_BADARG;
+    void* p = nullptr;
+    cudaError_t e;
+    {
+        std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
+        e = cudaGetSymbolAddress(&p, g_static_scratch);
     }
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            set_error("anl_dot_static: cudaGetSymbolAddress failed on device %d: %s", dev, cudaGetErrorString(e));
-            return ANL_ERR_CUDA;
-        }
-        g_scratch_ptr[dev] = p;
+    if (e != cudaSuccess || p == nullptr) {
+        int dev = -1;
+        cudaGetDevice(&dev);
+        set_error("anl_dot_static: cudaGetSymbolAddress failed on device %d: %s", dev, cudaGetErrorString(e));
+        return ANL_ERR_CUDA;
     }
-    *out = (double*)g_scratch_ptr[dev];
+    *out = (double*)p;
     return ANL_OK;
 }
 

@@ -5,7 +5,10 @@ arguments and return types (fem.py:20-263), so callers written for the reference
 unchanged. What changes underneath: there is no CSR matrix. ``FEM.assemble`` returns a
 lightweight operator that holds the element scales on the device, and ``FEM.solve`` runs
 the multigrid-preconditioned CG of the CUDA library (libanneal_gb300.so). Solves with
-rtol >= 1e-7 run in FP32 with FP64 CG scalars and solution; tighter tolerances run in FP64.
+rtol >= 1e-7 run in FP32 with FP64 CG scalars and solution; tighter tolerances run in FP64
+(``precision="fp32"`` or ``"fp64"`` forces one). FP32 solves certify their tolerance on
+the true residual of the FP64 operator; one that stops improving above its tolerance is
+finished by the FP64 solver.
 """
 import time
 
@@ -141,8 +144,11 @@ class StiffnessOperator:
 class FEM:
     """Linear elastic solve on the active voxels of a grid (fem.py:130-263)."""
 
-    def __init__(self, grid, active, fixed_dofs, nu, log=None):
+    def __init__(self, grid, active, fixed_dofs, nu, log=None, precision="auto"):
         require_cuda()
+        if precision not in ("auto", "fp32", "fp64"):
+            raise ValueError(f"precision must be 'auto', 'fp32' or 'fp64', not {precision!r}")
+        self.precision = precision
         t0 = time.time()
         self.grid = grid
         self.nu = float(nu)
@@ -207,10 +213,13 @@ class FEM:
         because the problem is linear; the remaining distinct cases run at the same time,
         each in its own context and stream, so the latency-bound coarse levels of their
         V-cycles overlap on the GPU."""
-        fp64 = rtol < FP32_RTOL_FLOOR
+        fp64 = self.fp64_for(rtol)
         nrhs = F.shape[0] if F.dim() == 2 else 1
         if nrhs == 1:
             st, iters, relres = self._ctx(fp64).solve(escale, F, X, rtol, maxiter, rebuild)
+            if st == N.ANL_ERR_STAGNATION:  # finish in FP64 from the FP32 iterate
+                st, it2, relres = self._ctx(True).solve(escale, F, X, rtol, maxiter, rebuild)
+                iters = [iters[0] + it2[0]]
             sts = [st]
         else:
             groups = self._multiple_groups(F, fp64)
@@ -227,9 +236,19 @@ class FEM:
             self.amg_builds += 1
         if any(st != N.ANL_OK for st in sts):
             raise SolverError(SOLVER_MESSAGE.format(maxiter=maxiter))
+        worst = max(relres)
+        if worst > rtol * (1 + 1e-9):
+            # only an FP64 solve at the attainable accuracy of its arithmetic gets here
+            self.log(f"  solve stopped at relative residual {worst:.2e} (FP64 floor; asked {rtol:.1e})")
         self.cg_iters.extend(iters)
         self.relres.extend(relres)
         return iters
+
+    def fp64_for(self, rtol):
+        """Whether a solve to ``rtol`` runs on the FP64 operator."""
+        if self.precision != "auto":
+            return self.precision == "fp64"
+        return rtol < FP32_RTOL_FLOOR
 
     def _multiple_groups(self, F, fp64):
         """[(representative, [(case, scale), ...]), ...]: cases whose load is a scalar
@@ -273,6 +292,10 @@ class FEM:
             with torch.cuda.stream(streams[k]):
                 r = reps[k]
                 st, it, rr = ctxs[k].solve(escale, F[r:r + 1], X[r:r + 1], rtol, maxiter, rebuild)
+                if st == N.ANL_ERR_STAGNATION:  # finish in FP64 from the FP32 iterate
+                    st, it2, rr = self._ctx(True, lane=k).solve(escale, F[r:r + 1], X[r:r + 1], rtol, maxiter,
+                                                                rebuild)
+                    it = [it[0] + it2[0]]
                 return st, it[0], rr[0]
         if len(reps) == 1:
             out = [work(0)]

@@ -8,8 +8,10 @@ already imported (or importable) ``anneal`` package: ``anneal.fem.FEM`` / ``Solv
 ``anneal.optimize.simp`` / ``Filter``, ``anneal.export.surface`` / ``output_field`` /
 ``choose_level`` / ``keep_load_paths`` / ``member_thickness``, the voxeliser
 (``anneal.geometry.voxel_fill`` and the names ``problem.py`` and ``run.py`` bound), the names ``run.py`` bound
-at import (``anneal.run.FEM``, ``anneal.run.simp`` and the export functions) and the validation
-gate's checks. Spec parsing, the other export steps, reports and the database stay the
+at import (``anneal.run.FEM``, ``anneal.run.simp`` and the export functions) and the solver
+names the validation gate bound at import (``anneal.validate.FEM`` / ``Grid`` /
+``hex8_matrices``), so the reference's own checks V1-V6 run against the GPU solver. Spec
+parsing, the other export steps, the gate itself, reports and the database stay the
 reference's.
 """
 import importlib
@@ -21,7 +23,6 @@ _EXPORT_NAMES = ("surface", "output_field", "choose_level", "keep_load_paths", "
 def install(anneal_pkg="anneal"):
     from . import fem as gfem
     from . import optimize as gopt
-    from . import validate as gval
     fem = importlib.import_module(f"{anneal_pkg}.fem")
     opt = importlib.import_module(f"{anneal_pkg}.optimize")
     fem.FEM = gfem.FEM
@@ -54,9 +55,10 @@ def install(anneal_pkg="anneal"):
         except ImportError:   # geometry.py needs trimesh
             pass
     try:
-        val = importlib.import_module(f"{anneal_pkg}.validate")
-        val.CHECKS = list(gval.CHECKS)
+        val = importlib.import_module(f"{anneal_pkg}.validate")   # validate.py:8 binds these by name
         val.FEM = gfem.FEM
+        val.Grid = gfem.Grid
+        val.hex8_matrices = gfem.hex8_matrices
     except ImportError:
         pass
     # keep the EMIN constant shared: the GPU simp reads anneal_gb300.optimize.EMIN

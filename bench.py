@@ -12,7 +12,8 @@ timed region), so both numbers sample the same SIMP iterations.
 
 N > 1 runs under torchrun with one independent replica per GPU (the solve has no
 cross-GPU exchange): value = total iterations / max rank time. ``--impl reference`` times
-the FP64 CPU oracle (the restatement of the reference's solver) on the host cores.
+the FP64 CPU oracle (the restatement of the reference's solver) on the host cores: W
+untimed and K timed SIMP iterations, each a full iteration with its PCG run to 1e-6.
 """
 import argparse
 import json
@@ -51,18 +52,6 @@ def read_peaks():
         return float(pk["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
-
-
-def profile_traffic():
-    """dram bytes per K u launch from the committed ncu summary, if there is one."""
-    path = os.path.join(ROOT, "profiles", "ku_apply_256x128x128.md")
-    try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_launch:"):
-                return float(line.split(":")[1].split()[0])
-    except OSError:
-        pass
-    return None
 
 
 class ClockSampler:
@@ -114,75 +103,61 @@ class ClockSampler:
                 "samples": len(rows), "reasons": reasons}
 
 
-# ------------------------------------------------------------------ CPU oracle sample
+# ------------------------------------------------------------------ CPU oracle
 
-def cpu_sample(w, n_cg, cg_sample=3):
-    """One SIMP iteration of the FP64 oracle at full size, with the CG cut to `cg_sample`
-    iterations and its per-iteration time scaled to `n_cg` (the GPU run's mean CG count).
-    Returns (seconds per SIMP iteration, threads, description)."""
+def oracle_run(w, iters):
+    """The FP64 oracle's SIMP loop on the workload, set up (FEM, filter) but not stepped:
+    each step() is one full iteration (filter, stiffness, multigrid set-up, PCG to RTOL from
+    the previous displacement, sensitivity, two filter backward passes, OC bisection)."""
     from oracle import oracle as O
     O.build()
+    return O.SimpRun(w.shape, w.h, w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, w.E0, w.nu, w.vf,
+                     iters=iters, r_mm=w.r_vox, p_final=3.0, move=0.2, x0=np.full(w.nelem, w.vf), beta_max=0.0,
+                     rtol=RTOL, emin=w.emin, log=lambda *a: None), O.num_threads()
+
+
+def cpu_sample(w):
+    """One full SIMP iteration of the FP64 oracle at full size (the first, from the initial
+    design). Returns (seconds, CG iterations, threads, description)."""
     t_all = time.perf_counter()
-    fem = O.OracleFEM(w.shape, w.h, w.active, w.fixed, w.nu)
-    filt = O.OracleFilter(w.shape, w.active, w.r_vox)
-    act = fem.act
-    phi = w.fill[act]
-    frz = w.frozen[act]
-    x = np.full(act.size, w.vf)
-    x[frz] = 1.0
+    run, threads = oracle_run(w, 1)
     t0 = time.perf_counter()
-    xp = filt.forward(x)
-    xp[frz] = 1.0
-    Ee = w.E0 * phi * (w.emin + xp ** 3 * (1 - w.emin))
-    F = np.where(fem.mask, w.loads["down"], 0.0)
-    t1 = time.perf_counter()
-    # the CG: setup + `cg_sample` iterations, then one more run of 1 iteration to separate
-    # the multigrid setup from the per-iteration cost
-    import ctypes
-    E = fem.full_E(Ee)
-    ts, u = [], None
-    for k in (1, cg_sample + 1):
-        u = np.zeros(3 * fem.nnode)
-        it, rr = ctypes.c_int(0), ctypes.c_double(0.0)
-        ta = time.perf_counter()
-        O.lib().orc_pcg(*fem.shape, O._p(fem.ke), O._p(E), O._p(fem.mask_u8, O._u8), O._p(F), O._p(u),
-                        1e-30, k, 1, 2, ctypes.byref(it), ctypes.byref(rr))
-        ts.append(time.perf_counter() - ta)
-    per_cg = (ts[1] - ts[0]) / cg_sample
-    setup = ts[0] - per_cg
-    t2 = time.perf_counter()
-    ce = fem.element_energy(u)
-    dc = -3 * xp ** 2 * (1 - w.emin) * w.E0 * phi * ce
-    dcx = filt.backward(np.minimum(dc, 0.0))
-    dvx = filt.backward(phi)
-    O.oc_update(filt, x, dcx, dvx, phi, frz, 0.2, 0.0, w.vf * phi.sum())
-    t3 = time.perf_counter()
-    per_iter = (t1 - t0) + setup + per_cg * n_cg + (t3 - t2)
-    desc = (f"one SIMP iteration of the FP64 oracle at 256x128x128: filter, stiffness, multigrid setup, "
-            f"{cg_sample} CG iterations scaled to {n_cg:.1f} (the GPU run's mean per solve), sensitivity, "
-            f"2 filter backward passes and the OC bisection; sample took {time.perf_counter() - t_all:.1f} s")
-    return per_iter, O.num_threads(), desc
+    rec = run.step()
+    t = time.perf_counter() - t0
+    cg = rec["cgIters"][0]
+    desc = (f"one full SIMP iteration (the first) of the FP64 oracle at 256x128x128: filter, stiffness, "
+            f"multigrid set-up, PCG to rel. residual {RTOL:g} ({cg} CG iterations), sensitivity, 2 filter "
+            f"backward passes, OC bisection; {t:.1f} s, {time.perf_counter() - t_all:.1f} s with set-up")
+    return t, cg, threads, desc
 
 
 # ------------------------------------------------------------------ arms
 
 def run_reference(args):
+    """The reference arm: the FP64 oracle's own SIMP loop on the host cores, W untimed
+    iterations, then K timed ones (wall clock per iteration; each a full iteration)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     w = make_workload()
-    n_cg = float(os.environ.get("ANL_BENCH_CG_ITERS", "40"))
-    times = []
-    for s in range(args.warmup + args.steps):
-        t, threads, desc = cpu_sample(w, n_cg)
-        if s >= args.warmup:
-            times.append(t)
-    tmean = float(np.mean(times))
-    value = 1.0 / tmean
+    run, threads = oracle_run(w, args.warmup + args.steps)
+    for _ in range(args.warmup):
+        run.step()
+    times, cgs = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rec = run.step()
+        times.append(time.perf_counter() - t0)
+        cgs.append(rec["cgIters"][0])
+    ttot = float(np.sum(times))
+    value = args.steps / ttot
+    desc = (f"SIMP iterations {args.warmup + 1}-{args.warmup + args.steps} of the FP64 oracle at 256x128x128, "
+            f"each in full: PCG to rel. residual {RTOL:g} from the previous displacement "
+            f"({np.mean(cgs):.1f} CG iterations per solve), filter, sensitivity, OC")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tmean, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * ttot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(), "cg_iters_per_solve": float(np.mean(cgs)),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -281,13 +256,13 @@ def run_gpu(args):
     alg_bytes = 24 * nn + 4 * ne
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     peak, peak_kind = read_peaks()
-    traffic = profile_traffic()
+    traffic = None  # DRAM bytes come from an ncu capture (profiles/), never from this timed run
     flops = 210.0 * ne  # modal element product: transforms, modal stiffness, node sums
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (FP64 CG scalars and solution)",
-                "data": "synthetic", "config": dict(workload_config(), parallelism=f"replicas x{world}"),
+                "data": "synthetic", "config": workload_config(), "parallelism": f"replicas x{world}",
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * w.nelem,
                         "d2h_bytes_per_step": 4 * w.nelem},
                 "gpu_launches": int(launches),
@@ -299,10 +274,9 @@ def run_gpu(args):
                              "ms_per_launch": ms, "fp32_tflops": flops / (ms * 1e-3) / 1e12},
                 "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:
-            n_cg = float(np.mean(cg_counts)) if cg_counts else 40.0
-            t, threads, desc = cpu_sample(w, n_cg)
+            t, cg, threads, desc = cpu_sample(w)
             line["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": desc}
+                                    "sample": desc, "cg_iters": cg}
         print(json.dumps(line), flush=True)
     run.close()
     if world > 1:

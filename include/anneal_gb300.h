@@ -32,7 +32,8 @@ enum {
     ANL_ERR_CUDA = 5,
     ANL_ERR_SINGULAR = 6, /* reserved (tiny coarse-grid pivots are regularised, not reported) */
     ANL_ERR_NOMEM = 7,
-    ANL_ERR_STATE = 8 /* a call that needs anl_set_domain / anl_filter_init came first */
+    ANL_ERR_STATE = 8, /* a call that needs anl_set_domain / anl_filter_init came first */
+    ANL_ERR_STAGNATION = 9 /* an FP32 solve stopped improving above rtol: finish it in FP64 */
 };
 
 enum { ANL_FLAG_FP64 = 1 /* K u, smoothers and CG vectors in FP64 (default: FP32) */ };
@@ -65,13 +66,20 @@ int anl_free_mask(anl_ctx* ctx, uint8_t* mask, anl_stream_t stream);
 int anl_apply_K(anl_ctx* ctx, const float* escale, const void* u, void* y, anl_stream_t stream);
 
 /* Replaces FEM.solve (fem.py:206-232): solves K x = f for nrhs right-hand sides, one after
-   another, by CG preconditioned with a geometric-multigrid V-cycle, each to
-   ||f - K x|| <= rtol ||f|| checked on the true residual. f and x are nrhs consecutive
-   nodal vectors (double); x holds the initial guesses on entry (x0_list). rebuild != 0
-   re-estimates the smoother spectra and refactors the coarse grid (the reference's AMG
-   rebuild, fem.py:207-216); otherwise the last ones are kept. iters / relres (host arrays
-   of nrhs) receive the CG iterations and final true relative residuals. Returns
-   ANL_ERR_MAXITER or ANL_ERR_NONFINITE where the reference raises SolverError. */
+   another, by CG preconditioned with a geometric-multigrid V-cycle. f and x are nrhs
+   consecutive nodal vectors (double); x holds the initial guesses on entry (x0_list).
+   rebuild != 0 re-estimates the smoother spectra and refactors the coarse grid (the
+   reference's AMG rebuild, fem.py:207-216); otherwise the last ones are kept. iters / relres
+   (host arrays of nrhs) receive the CG iterations and final true relative residuals
+   ||f - K x|| / ||f|| of the FP64 operator.
+   Acceptance: a solve returns ANL_OK when its true residual meets ||f - K x|| <= rtol ||f||.
+   The one exception is an FP64 context whose true residual has stopped falling at the
+   attainable accuracy of FP64 arithmetic: it also returns ANL_OK once another round of
+   iterations has not halved the residual, if relres <= max(100 rtol, 1e-10); relres then
+   exceeds rtol. An FP32 context never accepts above rtol: it returns ANL_ERR_STAGNATION
+   (x holds its best iterate) so the caller can finish the solve in an FP64 context.
+   Returns ANL_ERR_MAXITER, ANL_ERR_NONFINITE or ANL_ERR_BREAKDOWN where the reference raises
+   SolverError. */
 int anl_solve(anl_ctx* ctx, const float* escale, const double* f, double* x, int nrhs, double rtol,
               int maxiter, int rebuild, int* iters, double* relres, anl_stream_t stream);
 
@@ -136,16 +144,17 @@ int anl_design_stats(anl_ctx* ctx, const float* xold, const float* xnew, const f
 /* ---------------------------------------------------------------- allocation-free variant */
 
 /* No counterpart in the reference. The compliance dot product of anl_dot (sum of a[i]*b[i],
-   FP64, deterministic) for callers that cannot allocate device memory: code inside a CUDA
-   host callback or memory-pool hook, embedders whose framework owns the whole device pool,
-   and loops that must not allocate (or synchronise) mid-step. It needs no context: a, b
-   (n doubles) and out (one double) are caller-owned device buffers; the result is written
-   to *out on `stream`. The reduction scratch is a fixed 33 KB array in the library's device
-   memory, held by every GPU that loads the library until the process exits; n may be at
-   most 268,435,456 (ANL_ERR_BADARG beyond). The first call on a device looks up that array's
-   device address (cudaGetSymbolAddress), so make it before any stream capture. Calls share
-   the array: calls that overlap on the GPU (other streams, other threads) race. Allocates
-   nothing, frees nothing. */
+   FP64, deterministic) for callers that cannot allocate device memory: a memory-pool hook or
+   allocator callback, embedders whose framework owns the whole device pool, and loops that
+   must not allocate (or synchronise) mid-step. It needs no context: a, b (n doubles) and out
+   (one double) are caller-owned device buffers; the result is written to *out on `stream`.
+   The reduction scratch is a fixed 33 KB array in the library's device memory, held by every
+   GPU that loads the library until the process exits; n may be at most 268,435,456
+   (ANL_ERR_BADARG beyond). Every call looks up that array's device address in the current
+   context (cudaGetSymbolAddress, which loads the library's module on a device's first call),
+   so make the first call on a device before any stream capture. Calls share the array:
+   calls that overlap on the GPU (other streams, other threads) race. Allocates nothing,
+   frees nothing. */
 int anl_dot_static(const double* a, const double* b, int64_t n, double* out, anl_stream_t stream);
 
 /* Replaces FEM.stress / FEM.von_mises (fem.py:244-263): element-centre stress sigma = E D B0 u_e

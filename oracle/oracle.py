@@ -212,109 +212,140 @@ def oc_update(filt, x, dcx, dvx, phi, frz, move, beta, vtarget):
     return xd, steps
 
 
-def simp(shape, h, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=80, r_mm=None,
-         p_final=3.0, move=0.2, combine="sum", log=print, tol=0.01, x0=None, beta_max=BETA_MAX,
-         rtol=1e-6, emin=None, precond="mg", maxiter=2000):
-    """optimize.py:50-180 restated. ``rtol`` is the CG tolerance the reference hard-codes
-    at optimize.py:122 (1e-6); ``emin`` overrides EMIN (optimize.py:18)."""
-    EM = EMIN if emin is None else emin
-    t_start = time.time()
-    fem = OracleFEM(shape, h, active, fixed, nu)
-    act = fem.act
-    phi = fill[act]
-    frz = frozen[act].astype(bool)
-    des = ~frz
-    r_vox = max((r_mm or 1.5 * h) / h, 1.5)
-    filt = OracleFilter(shape, active, r_vox)
-    cases = list(loads)
-    Fr = [np.where(fem.mask, loads[c], 0.0) for c in cases]
-    w = np.array([weights[c] for c in cases])
-    if all(np.allclose(f, 0) for f in Fr):
-        raise ValueError("All loads are zero after mapping onto the grid. Check the load anchors' regions.")
-    Vtot = phi.sum()
-    Vtarget = vf * Vtot
-    Vfrozen = phi[frz].sum()
-    x = np.ones(act.size)
-    x[des] = np.clip((Vtarget - Vfrozen) / max(phi[des].sum(), 1e-12), 0.01, 1.0)
-    warm = x0 is not None
-    if warm:
-        xs = np.clip(x0[act], 0.0, 1.0)
-        cur = (phi[des] * xs[des]).sum()
-        if cur > 0:
-            x[des] = np.clip(xs[des] * (Vtarget - Vfrozen) / cur, 0.001, 1.0)
-    beta = [0.0]
+class SimpRun:
+    """The state of one oracle SIMP run (optimize.py:50-104) and one ``step()`` per iteration
+    (optimize.py:105-172). ``simp`` drives it; the CPU baseline of the benchmark times
+    ``step()`` directly."""
 
-    def project(xt):
-        b = beta[0]
+    def __init__(self, shape, h, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=80, r_mm=None,
+                 p_final=3.0, move=0.2, combine="sum", log=print, x0=None, beta_max=BETA_MAX, rtol=1e-6,
+                 emin=None, precond="mg", maxiter=2000):
+        self.EM = EMIN if emin is None else emin
+        self.shape, self.h = tuple(int(s) for s in shape), h
+        self.E0, self.vf, self.iters, self.p_final, self.move = E0, vf, iters, p_final, move
+        self.combine, self.log, self.beta_max, self.rtol = combine, log, beta_max, rtol
+        self.precond, self.maxiter = precond, maxiter
+        self.fem = fem = OracleFEM(shape, h, active, fixed, nu)
+        act = self.act = fem.act
+        self.phi = phi = np.asarray(fill, float)[act]
+        self.frz = frz = np.asarray(frozen)[act].astype(bool)
+        self.des = des = ~frz
+        self.r_vox = max((r_mm or 1.5 * h) / h, 1.5)
+        self.filt = OracleFilter(shape, active, self.r_vox)
+        self.cases = cases = list(loads)
+        self.Fr = [np.where(fem.mask, loads[c], 0.0) for c in cases]
+        self.w = np.array([weights[c] for c in cases])
+        if all(np.allclose(f, 0) for f in self.Fr):
+            raise ValueError("All loads are zero after mapping onto the grid. Check the load anchors' regions.")
+        self.Vtot = phi.sum()
+        self.Vtarget = vf * self.Vtot
+        Vfrozen = phi[frz].sum()
+        x = np.ones(act.size)
+        x[des] = np.clip((self.Vtarget - Vfrozen) / max(phi[des].sum(), 1e-12), 0.01, 1.0)
+        self.warm = x0 is not None
+        if self.warm:
+            xs = np.clip(np.asarray(x0)[act], 0.0, 1.0)
+            cur = (phi[des] * xs[des]).sum()
+            if cur > 0:
+                x[des] = np.clip(xs[des] * (self.Vtarget - Vfrozen) / cur, 0.001, 1.0)
+        self.x = x
+        self.beta = beta_max / 2 if self.warm else 0.0
+        self.hist = []
+        self.U = [None] * len(cases)
+        self.c0 = None
+        self.p = 1.0
+        self.xPhys = self.physical(x)
+        self.beta_step = max(5, int(0.12 * iters))
+        self.beta_since = 0
+        self.it = 0
+
+    def project(self, xt):
+        b = self.beta
         if b <= 0:
             return xt, np.ones_like(xt)
         t0, t1 = np.tanh(b * ETA), np.tanh(b * (1 - ETA))
         th = np.tanh(b * (xt - ETA))
         return (t0 + th) / (t0 + t1), b * (1 - th ** 2) / (t0 + t1)
 
-    def physical(xd, with_grad=False):
-        xt = filt.forward(xd)
-        xp, dxp = project(xt)
-        xp[frz] = 1.0
+    def physical(self, xd, with_grad=False):
+        xt = self.filt.forward(xd)
+        xp, dxp = self.project(xt)
+        xp[self.frz] = 1.0
         return (xp, dxp) if with_grad else xp
 
-    hist = []
-    U = [None] * len(cases)
-    c0 = None
-    p = 1.0
-    if warm:
-        beta[0] = beta_max / 2
-    xPhys = physical(x)
-    beta_step = max(5, int(0.12 * iters))
-    beta_since = 0
-    for it in range(1, iters + 1):
+    def step(self):
         t0 = time.time()
+        self.it += 1
+        it, iters, p_final, EM, E0 = self.it, self.iters, self.p_final, self.EM, self.E0
+        fem, phi, frz, des, w = self.fem, self.phi, self.frz, self.des, self.w
         hold = max(1, min(3, int(0.4 * iters / max((p_final - 1.0) / 0.25, 1))))
-        p = p_final if warm else min(p_final, 1.0 + 0.25 * ((it - 1) // hold))
-        if p >= p_final and not warm and beta_max > 0:
-            if beta[0] == 0:
-                beta[0], beta_since = 1.0, 0
-            elif beta_since >= beta_step and beta[0] < beta_max:
-                beta[0], beta_since = min(beta_max, 2 * beta[0]), 0
-            beta_since += 1
-        xPhys, dxp = physical(x, with_grad=True)
+        p = self.p = p_final if self.warm else min(p_final, 1.0 + 0.25 * ((it - 1) // hold))
+        if p >= p_final and not self.warm and self.beta_max > 0:
+            if self.beta == 0:
+                self.beta, self.beta_since = 1.0, 0
+            elif self.beta_since >= self.beta_step and self.beta < self.beta_max:
+                self.beta, self.beta_since = min(self.beta_max, 2 * self.beta), 0
+            self.beta_since += 1
+        xPhys, dxp = self.physical(self.x, with_grad=True)
         Ee = E0 * phi * (EM + xPhys ** p * (1 - EM))
-        U = fem.solve(Ee, Fr, x0_list=None if U[0] is None else U, rtol=rtol, maxiter=maxiter,
-                      precond=precond)
-        cs = np.array([f @ u for f, u in zip(Fr, U)])
+        U = self.U = fem.solve(Ee, self.Fr, x0_list=None if self.U[0] is None else self.U, rtol=self.rtol,
+                               maxiter=self.maxiter, precond=self.precond)
+        cs = np.array([f @ u for f, u in zip(self.Fr, U)])
         dce = []
         for u in U:
             ce = fem.element_energy(u)
             dce.append(-p * xPhys ** (p - 1) * (1 - EM) * E0 * phi * ce)
-        if c0 is None:
-            c0 = cs.copy()
-        if combine == "sum" or len(cases) == 1:
+        if self.c0 is None:
+            self.c0 = cs.copy()
+        if self.combine == "sum" or len(self.cases) == 1:
             obj = float(w @ cs)
             dc = sum(wi * d for wi, d in zip(w, dce))
         else:
-            r = w * cs / c0
+            r = w * cs / self.c0
             obj = float((r ** PNORM).sum() ** (1 / PNORM))
-            coef = (r / obj) ** (PNORM - 1) * w / c0
+            coef = (r / obj) ** (PNORM - 1) * w / self.c0
             dc = sum(ci * d for ci, d in zip(coef, dce))
         dc = np.minimum(dc, 0.0)
-        dcx = filt.backward(dc * dxp)
-        dvx = filt.backward(phi * dxp)
-        xd, _ = oc_update(filt, x, dcx, dvx, phi, frz, move, beta[0], Vtarget)
-        change = float(np.abs(xd - x)[des].max()) if des.any() else 0.0
-        x = xd
-        xPhys = physical(x)
+        dcx = self.filt.backward(dc * dxp)
+        dvx = self.filt.backward(phi * dxp)
+        xd, _ = oc_update(self.filt, self.x, dcx, dvx, phi, frz, self.move, self.beta, self.Vtarget)
+        change = float(np.abs(xd - self.x)[des].max()) if des.any() else 0.0
+        self.x = xd
+        self.xPhys = xPhys = self.physical(xd)
         grey = float(((xPhys > 0.1) & (xPhys < 0.9))[des].mean()) if des.any() else 0.0
-        hist.append({"iter": it, "objective": obj, "compliance": cs.tolist(), "p": p, "beta": beta[0],
-                     "volumeFraction": float((phi * xPhys).sum() / Vtot), "change": change,
-                     "grey": grey, "cgIters": fem.cg_iters[-len(cases):], "amgRebuilt": True,
-                     "seconds": time.time() - t0})
-        log(f"  it {it:3d}  p {p:.2f}  b {beta[0]:.0f}  obj {obj:.4g}  vol {hist[-1]['volumeFraction']:.3f}  "
-            f"change {change:.3f}  grey {grey:.2f}  cg {fem.cg_iters[-1]} amg  "
-            f"{hist[-1]['seconds']:.1f}s")
-        if p >= p_final and beta[0] >= beta_max and it > (5 if warm else 10) and change < tol:
-            log(f"  converged at iteration {it}")
+        rec = {"iter": it, "objective": obj, "compliance": cs.tolist(), "p": p, "beta": self.beta,
+               "volumeFraction": float((phi * xPhys).sum() / self.Vtot), "change": change,
+               "grey": grey, "cgIters": fem.cg_iters[-len(self.cases):], "amgRebuilt": True,
+               "seconds": time.time() - t0}
+        self.hist.append(rec)
+        self.log(f"  it {it:3d}  p {p:.2f}  b {self.beta:.0f}  obj {obj:.4g}  vol {rec['volumeFraction']:.3f}  "
+                 f"change {change:.3f}  grey {grey:.2f}  cg {fem.cg_iters[-1]} amg  {rec['seconds']:.1f}s")
+        return rec
+
+    def converged(self, tol):
+        rec = self.hist[-1]
+        return (rec["p"] >= self.p_final and rec["beta"] >= self.beta_max
+                and self.it > (5 if self.warm else 10) and rec["change"] < tol)
+
+    def full_x(self):
+        full = np.zeros(int(np.prod(self.shape)))
+        full[self.act] = self.xPhys
+        return full
+
+
+def simp(shape, h, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=80, r_mm=None,
+         p_final=3.0, move=0.2, combine="sum", log=print, tol=0.01, x0=None, beta_max=BETA_MAX,
+         rtol=1e-6, emin=None, precond="mg", maxiter=2000):
+    """optimize.py:50-180 restated. ``rtol`` is the CG tolerance the reference hard-codes
+    at optimize.py:122 (1e-6); ``emin`` overrides EMIN (optimize.py:18)."""
+    t_start = time.time()
+    run = SimpRun(shape, h, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=iters, r_mm=r_mm,
+                  p_final=p_final, move=move, combine=combine, log=log, x0=x0, beta_max=beta_max, rtol=rtol,
+                  emin=emin, precond=precond, maxiter=maxiter)
+    for _ in range(iters):
+        run.step()
+        if run.converged(tol):
+            log(f"  converged at iteration {run.it}")
             break
-    full = np.zeros(int(np.prod(shape)))
-    full[act] = xPhys
-    return {"x": full, "history": hist, "fem_builds": len(hist), "rMM": r_vox * h,
-            "seconds": time.time() - t_start, "cases": cases, "U": U}
+    return {"x": run.full_x(), "history": run.hist, "fem_builds": len(run.hist), "rMM": run.r_vox * h,
+            "seconds": time.time() - t_start, "cases": run.cases, "U": run.U}

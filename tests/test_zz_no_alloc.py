@@ -1,7 +1,7 @@
 """The allocation-free compliance dot product (anl_dot_static) against anl_dot.
 
-anl_dot_static exists for callers that cannot allocate device memory (host callbacks,
-memory-pool hooks, frameworks that own the whole pool): it keeps its reduction scratch in
+anl_dot_static exists for callers that cannot allocate device memory (memory-pool hooks
+and allocator callbacks, frameworks that own the whole pool): it keeps its reduction scratch in
 a fixed array inside the library. This test calls it through the C ABI twice in a row on
 different data and compares each result with the context-based anl_dot, at the FP64
 tolerance the other dot-product tests use. It sits in its own file, collected last."""
