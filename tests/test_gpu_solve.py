@@ -183,7 +183,10 @@ def test_bench_workload_lbracket_256_fp32_first_iterations_match_oracle(golden):
     s, c, vol, x = _lbracket_run(golden, "lbracket256_3it.npz", 4.0 / 3.0)
     assert np.abs(c / s["h_compliance"] - 1).max() < 1e-5
     assert np.abs(vol - s["h_volumeFraction"]).max() < 1e-5
-    assert np.abs(x - s["x_q16"] / 65535.0).max() < 1e-3
+    # every 17th element at the density bar; every element through its x-row's sum
+    assert np.abs(x[::17] - s["x_q16_stride17"] / 65535.0).max() < 1e-3
+    nx = int(s["shape"][0])
+    assert np.abs(x.reshape(-1, nx).sum(axis=1) - s["row_sums"]).max() < 1e-3 * nx
 
 
 def test_log_line_format_matches_reference(golden):
