@@ -35,7 +35,7 @@ EXPORTS = [
     "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
     "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam", "anl_element_stress",
     "anl_vox_create", "anl_vox_destroy", "anl_voxel_fill", "anl_output_field", "anl_choose_level",
-    "anl_label_above", "anl_edt",
+    "anl_label_above", "anl_edt", "anl_profile_pass",
 ]
 
 
@@ -74,6 +74,7 @@ _SIGS = {
     "anl_oc_update": (I, [P, P, P, P, P, P, D, D, D, D, P, ctypes.POINTER(I), ctypes.POINTER(D), P]),
     "anl_design_stats": (I, [P, P, P, P, P, P, ctypes.POINTER(D), P]),
     "anl_profile_apply": (I, [P, P, P, I, ctypes.POINTER(D), P]),
+    "anl_profile_pass": (I, [P, I, I, ctypes.POINTER(D), P]),
     "anl_launch_count": (I64, []),
     "anl_mg_info": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)]),
     "anl_dot_static": (I, [P, P, I64, P, P]),

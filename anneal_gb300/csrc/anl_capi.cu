@@ -191,6 +191,7 @@ int design_stats(anl_ctx* c, const float* xold, const float* xnew, const float* 
 int ku_grid_blocks(const Dims& d);
 void ku_prepare();
 int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* ms, cudaStream_t s);
+int solver_profile_pass(anl_ctx* c, int pass, int reps, double* ms, cudaStream_t s);
 
 // ------------------------------------------------------------------ context
 
@@ -394,8 +395,13 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     }
     c->use_graph = std::getenv("ANL_NO_GRAPH") == nullptr;
     if (const char* e = std::getenv("ANL_BOX_FROM")) c->box_from = std::atoi(e);
+    if (const char* e = std::getenv("ANL_TC")) c->use_tc = !c->fp64 && std::atoi(e) != 0;
     ku_prepare();
     kbox_prepare();
+    if (c->use_tc && kutc_prepare(c->ke) != ANL_OK) {
+        free_ctx(c);
+        return ANL_ERR_CUDA;
+    }
     if (cudaMallocHost((void**)&c->sc_h, sizeof(PcgScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->red_h, 16 * sizeof(double)) != cudaSuccess) {
         set_error("pinned host allocation failed");
@@ -567,6 +573,15 @@ int anl_profile_apply(anl_ctx* ctx, const void* u, void* y, int reps, double* ms
         return ANL_ERR_STATE;
     }
     return solver_profile_apply(ctx, u, y, reps, ms_h, S(stream));
+}
+
+int anl_profile_pass(anl_ctx* ctx, int pass, int reps, double* ms_h, anl_stream_t stream) {
+    NEED(ctx && ms_h && reps >= 1, "anl_profile_pass: bad argument");
+    if (!ctx->domain_set || !ctx->coarse_ready) {
+        set_error("anl_profile_pass: run a solve on this context first");
+        return ANL_ERR_STATE;
+    }
+    return solver_profile_pass(ctx, pass, reps, ms_h, S(stream));
 }
 
 int anl_mg_info(anl_ctx* ctx, int* nlev_h, int* dims_h, double* lmax_h) {

@@ -77,6 +77,8 @@ struct anl_ctx {
     // first level smoothed by the box kernels (anl_kbox.cu; FP32 contexts): on the levels below
     // 128 x 64 x 64 elements a z-marching K u launch is a chain of latencies
     int box_from = 2;
+    // the finest level's K u passes on the tensor cores (anl_kutc.cu; FP32 contexts)
+    bool use_tc = false;
 #ifndef ANL_CHEB_LO
 #define ANL_CHEB_LO 0.03
 #endif

@@ -7,6 +7,30 @@ namespace anl {
 
 // ------------------------------------------------------------------ K u family
 
+// u . (K u) accumulators of the APPLY_DOT passes (and ||r||^2 of the accurate residual)
+template <class T>
+struct DotAcc;
+template <>
+struct DotAcc<float> {
+    Acc2 a;
+    __device__ void add(float x, float y) { a.add_prod(x, y); }
+    __device__ double value() const { return a.value(); }
+};
+template <>
+struct DotAcc<double> {
+    double s = 0.0;
+    __device__ void add(double x, double y) { s = fma(x, y, s); }
+    __device__ double value() const { return s; }
+};
+template <>
+struct DotAcc<DF> {  // the accurate residual: ||r||^2 of its FP32 values, compensated
+    Acc2 a;
+    __device__ void add(DF x, DF y) { a.add_prod(x.hi + x.lo, y.hi + y.lo); }
+    __device__ void add_sq(float v) { a.add_prod(v, v); }
+    __device__ double value() const { return a.value(); }
+};
+
+
 // KU_CHEB0: the first two Chebyshev steps from x = 0 in one pass: x1 = c2_0 D^-1 b is formed
 // on the fly from the staged b and diagonal, then x2 = x1 + c1_1 x1 + c2_1 D^-1 (b - K x1)
 enum { KU_APPLY = 0, KU_APPLY_DOT = 1, KU_RESID = 2, KU_CHEB = 3, KU_CHEB0 = 4 };
@@ -72,6 +96,16 @@ struct KbArgs {
 
 int launch_kbox(int mode, const KbArgs& a, const KeModal<float>& km, cudaStream_t s);
 void kbox_prepare();
+
+// ------------------------------------------------------------------ tensor-core K u (fine grid)
+
+// The FP32 K u passes KU_APPLY, KU_APPLY_DOT, KU_RESID and KU_CHEB on the tensor cores
+// (anl_kutc.cu): the edge-difference form of the element product as TF32 MMAs with a
+// three-product split. kutc_prepare builds the constant operand from Ke (unit cube) once per
+// device; kutc_error_flag reads the flag a kernel sets when one of its waits gave up.
+int kutc_prepare(const double* ke);
+int launch_kutc(int mode, const KuArgs<float>& a, const KeModal<float>& km, cudaStream_t s);
+int kutc_error_flag(int* out_h);
 
 
 }  // namespace anl

@@ -42,28 +42,6 @@ namespace anl {
 
 __host__ __device__ constexpr int ceil_div_d(int a, int b) { return (a + b - 1) / b; }
 
-template <class T>
-struct DotAcc;
-template <>
-struct DotAcc<float> {
-    Acc2 a;
-    __device__ void add(float x, float y) { a.add_prod(x, y); }
-    __device__ double value() const { return a.value(); }
-};
-template <>
-struct DotAcc<double> {
-    double s = 0.0;
-    __device__ void add(double x, double y) { s = fma(x, y, s); }
-    __device__ double value() const { return s; }
-};
-template <>
-struct DotAcc<DF> {  // the accurate residual: ||r||^2 of its FP32 values, compensated
-    Acc2 a;
-    __device__ void add(DF x, DF y) { a.add_prod(x.hi + x.lo, y.hi + y.lo); }
-    __device__ void add_sq(float v) { a.add_prod(v, v); }
-    __device__ double value() const { return a.value(); }
-};
-
 // node-field loads of the epilogue
 __device__ __forceinline__ float ldg_t(const float* p) { return __ldg(p); }
 __device__ __forceinline__ double ldg_t(const double* p) { return __ldg(p); }

@@ -736,6 +736,20 @@ KeModal<float> modal_of<float>(const anl_ctx* c) { return c->kmf; }
 template <>
 KeModal<double> modal_of<double>(const anl_ctx* c) { return c->kmd; }
 
+// The K u passes of the finest level go to the tensor-core kernel (anl_kutc.cu) when the
+// context enables it (FP32 contexts); every other level and precision uses the SIMT kernel.
+template <class T>
+static int ku_pass(anl_ctx* c, const Level& L, int mode, const KuArgs<T>& a, cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        if (c->use_tc && &L == &c->lev[0]) {
+            KuArgs<float> t = a;
+            t.diag = L.diag;
+            return launch_kutc(mode, t, c->kmf, s);
+        }
+    }
+    return launch_ku<T>(mode, a, modal_of<T>(c), s);
+}
+
 template <class T>
 static KuArgs<T> ku_args(anl_ctx* c, const Level& L) {
     KuArgs<T> a;
@@ -757,7 +771,7 @@ static int apply_level(anl_ctx* c, const Level& L, const T* u, T* y, cudaStream_
     a.y = y;
     a.done = done;
     a.red_out = dot_out;
-    return launch_ku<T>(dot_out ? KU_APPLY_DOT : KU_APPLY, a, modal_of<T>(c), s);
+    return ku_pass<T>(c, L, dot_out ? KU_APPLY_DOT : KU_APPLY, a, s);
 }
 
 static int level_index(const anl_ctx* c, const Level& L) { return (int)(&L - &c->lev[0]); }
@@ -869,7 +883,7 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
         a.c1_zero = k == 0;
         a.dv_keep = k + 1 < degree;
         a.done = done;
-        ANL_TRY(launch_ku<T>(KU_CHEB, a, modal_of<T>(c), s));
+        ANL_TRY(ku_pass<T>(c, L, KU_CHEB, a, s));
         std::swap(L.x, L.xt);
     }
     return ANL_OK;
@@ -968,7 +982,7 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     a.b = (const T*)L.b;
     a.y = (T*)L.r;
     a.done = done;
-    ANL_TRY(launch_ku<T>(KU_RESID, a, modal_of<T>(c), s));
+    ANL_TRY(ku_pass<T>(c, L, KU_RESID, a, s));
     k_restrict<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<T>(c, l + 1, done, s));
@@ -1295,6 +1309,47 @@ int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, in
     if (worst == ANL_ERR_STAGNATION)
         set_error("FP32 CG stopped improving above rtol %.3g (finish the solve in FP64)", rtol);
     return worst;
+}
+
+// Times one finest-level pass of the solve, `reps` launches between two CUDA events on s, on
+// the context's own work vectors (their contents are whatever the last solve left; the timed
+// passes overwrite the V-cycle scratch, which the next solve re-initialises). FP32 contexts.
+int solver_profile_pass(anl_ctx* c, int pass, int reps, double* ms, cudaStream_t s) {
+    if (c->fp64) {
+        set_error("profile pass: FP32 contexts only");
+        return ANL_ERR_BADARG;
+    }
+    Level& L = c->lev[0];
+    const double* cf = c->cheb_d + 1;  // level 0 (c1, c2) pairs
+    KuArgs<float> a = ku_args<float>(c, L);
+    int mode = KU_APPLY;
+    switch (pass) {
+        case 0: a.u = (const float*)c->p; a.y = (float*)c->q; mode = KU_APPLY; break;
+        case 1: a.u = (const float*)c->p; a.y = (float*)c->q; a.red_out = c->red_out + 12; mode = KU_APPLY_DOT; break;
+        case 2: a.u = (const float*)L.x; a.b = (const float*)L.b; a.y = (float*)L.r; mode = KU_RESID; break;
+        case 3:
+            a.u = (const float*)L.x; a.b = (const float*)L.b; a.dv = (float*)L.dv; a.xout = (float*)L.xt;
+            a.cheb = cf + 2; a.c1_zero = 0; a.dv_keep = 0; mode = KU_CHEB;  // the last step of a sweep
+            break;
+        case 4:
+            a.b = (const float*)L.b; a.diag = L.diag; a.dv = (float*)L.dv; a.xout = (float*)L.x;
+            a.cheb0 = cf; a.cheb = cf + 2; a.dv_keep = 1; mode = KU_CHEB0;
+            break;
+        default: set_error("profile pass: unknown pass %d", pass); return ANL_ERR_BADARG;
+    }
+    cudaEvent_t e0, e1;
+    ANL_CUDA(cudaEventCreate(&e0));
+    ANL_CUDA(cudaEventCreate(&e1));
+    ANL_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps; ++r) ANL_TRY(ku_pass<float>(c, L, mode, a, s));
+    ANL_CUDA(cudaEventRecord(e1, s));
+    ANL_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    ANL_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = (double)t / reps;
+    return ANL_OK;
 }
 
 int solver_profile_apply(anl_ctx* c, const void* u, void* y, int reps, double* ms, cudaStream_t s) {

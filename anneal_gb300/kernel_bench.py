@@ -34,7 +34,11 @@ def main():
     ap.add_argument("--export", action="store_true")
     ap.add_argument("--voxel", action="store_true")
     ap.add_argument("--subdiv", type=int, default=6)
+    ap.add_argument("--tc", action="store_true", help="the tensor-core K u kernel (FP32)")
     a = ap.parse_args()
+    if a.tc:
+        import os
+        os.environ["ANL_TC"] = "1"
     if a.export:
         return export_bench(a.shape, a.reps)
     if a.voxel:
@@ -56,7 +60,8 @@ def main():
     ctx.apply_K(E, u, y)
     ms = ctx.profile_apply(u, y, a.reps)
     alg = 24 * nn + 4 * ne
-    print(json.dumps({"kernel": "K u (APPLY)", "shape": [nx, ny, nz], "precision": "fp64" if a.fp64 else "fp32",
+    print(json.dumps({"kernel": "K u (APPLY)" + (" tensor cores" if a.tc else ""), "shape": [nx, ny, nz],
+                      "precision": "fp64" if a.fp64 else "fp32",
                       "ms_per_launch": ms, "algorithmic_bytes": alg, "GBps": alg / (ms * 1e-3) / 1e9,
                       "tflops": MODAL_FLOPS * ne / (ms * 1e-3) / 1e12}))
     ctx.close()

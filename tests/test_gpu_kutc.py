@@ -1,0 +1,100 @@
+"""The tensor-core K u (tcgen05, three-product TF32 split of the edge-difference form) against
+the FP64 oracle and against the SIMT kernel, through the C ABI.
+
+The kernel serves the finest grid of FP32 contexts created with ANL_TC=1. Shapes cover one and
+several 128-element x-tiles, a grid that ends exactly on a tile (node nx owned by the tile's last
+thread), partial y-tiles and z-segments. Bar: 2e-6 of the largest |K u| (the FP32 SIMT bar)."""
+import numpy as np
+import pytest
+import torch
+
+from anneal_gb300.context import Context, to_dev
+
+pytestmark = pytest.mark.gpu
+
+F32, U8 = torch.float32, torch.uint8
+
+
+def _domain(shape, seed):
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    ne = nx * ny * nz
+    e = np.arange(ne)
+    i, k = e % nx, e // (nx * ny)
+    active = ~((i >= nx // 2) & (k >= nz // 2)) & (rng.random(ne) > 0.1)
+    nn = (nx + 1) * (ny + 1) * (nz + 1)
+    n = np.arange(nn)
+    fixed = np.zeros(3 * nn, np.uint8)
+    c = n[n % (nx + 1) == 0]
+    fixed[3 * c] = fixed[3 * c + 1] = fixed[3 * c + 2] = 1
+    E = np.exp(rng.normal(0.0, 1.0, ne))
+    E[rng.random(ne) < 0.2] = 1e-9
+    E[~active] = 0.0
+    return active, fixed, E
+
+
+def _apply(shape, active, fixed, E, u, tc, monkeypatch):
+    monkeypatch.setenv("ANL_TC", "1" if tc else "0")
+    c = Context(shape, 1.0, 0.3)
+    c.set_domain(to_dev(active.astype(np.uint8), U8), to_dev(fixed, U8))
+    y = torch.empty(c.ndof, dtype=F32, device="cuda")
+    c.apply_K(to_dev(E, F32), to_dev(u, F32), y)
+    out = y.cpu().numpy().astype(float)
+    c.close()
+    return out
+
+
+@pytest.mark.parametrize("shape", [(7, 5, 4), (128, 9, 6), (130, 15, 9), (200, 10, 7), (256, 16, 12)])
+def test_tc_apply_matches_oracle(oracle, shape, monkeypatch):
+    active, fixed, E = _domain(shape, seed=sum(shape))
+    fem = oracle.OracleFEM(shape, 1.0, active, np.flatnonzero(fixed), 0.3)
+    rng = np.random.default_rng(2)
+    u = np.where(fem.mask, rng.normal(0.0, 1.0, 3 * fem.nnode), 0.0)
+    want = fem.apply(E[fem.act], u)
+    got = _apply(shape, active, fixed, E, u, True, monkeypatch)
+    assert np.abs(got - want).max() <= 2e-6 * np.abs(want).max()
+
+
+def test_tc_apply_on_a_smooth_field_matches_simt(oracle, monkeypatch):
+    """A smooth displacement (rigid translation plus a long-wave bend): large |u|, small strain.
+    The edge-difference form keeps the tensor-core result as close to the FP64 operator as the
+    SIMT kernel's."""
+    shape = (160, 12, 10)
+    active, fixed, E = _domain(shape, seed=11)
+    fem = oracle.OracleFEM(shape, 1.0, active, np.flatnonzero(fixed), 0.3)
+    nx, ny, nz = shape
+    n = np.arange(fem.nnode)
+    x = (n % (nx + 1)) / nx
+    u = np.zeros((fem.nnode, 3))
+    u[:, 0] = 5.0 + 0.01 * np.sin(np.pi * x)
+    u[:, 2] = 3.0 - 0.02 * x ** 2
+    u = np.where(fem.mask, u.ravel(), 0.0)
+    want = fem.apply(E[fem.act], u)
+    tc = _apply(shape, active, fixed, E, u, True, monkeypatch)
+    simt = _apply(shape, active, fixed, E, u, False, monkeypatch)
+    err_tc = np.abs(tc - want).max()
+    err_simt = np.abs(simt - want).max()
+    assert err_tc <= 4 * err_simt + 1e-7 * np.abs(want).max(), (err_tc, err_simt)
+
+
+@pytest.mark.parametrize("mode", ["fp32"])
+def test_tc_engine_solve_matches_simt_engine(monkeypatch, mode):
+    """A whole multigrid-preconditioned solve with the finest level's passes (K p with p.Kp, the
+    residual, the Chebyshev steps) on the tensor cores gives the SIMT engine's solution to the
+    tolerance, in about as many CG iterations."""
+    from anneal_gb300 import fem as G
+    from anneal_gb300 import problems as P
+    w = P.cantilever(256, 16, 12)
+    rho = P.random_density(w.shape, 4)
+    out = {}
+    for tc in (True, False):
+        monkeypatch.setenv("ANL_TC", "1" if tc else "0")
+        fem = G.FEM(G.Grid(w.shape, 1.0, (0, 0, 0)), w.active, w.fixed, 0.3, precision=mode)
+        Ee = 1e-9 + rho[fem.act] ** 3 * (1 - 1e-9)
+        u = fem.solve(fem.assemble(Ee), [fem.reduce_load(w.loads["c"])], rtol=1e-8)[0]
+        out[tc] = (u, fem.cg_iters[-1], fem.relres[-1])
+        fem.close()
+    (ut, it_t, rr_t), (us, it_s, rr_s) = out[True], out[False]
+    assert rr_t <= 1e-8 and rr_s <= 1e-8
+    assert np.abs(ut - us).max() <= 1e-6 * np.abs(us).max()
+    assert abs(it_t - it_s) <= max(2, it_s // 10), (it_t, it_s)
