@@ -325,6 +325,44 @@ __device__ __forceinline__ void block_sum(double (&val)[NV], double* smem /* NV*
     }
 }
 
+// The same block sum for values given as unevaluated float pairs (s + c) per thread: the warp
+// tree adds pairs with TwoSum on the FP32 pipes (FP64 arithmetic on this part runs at a small
+// fraction of FP32, and a tree of FP64 adds over every thread of a full grid costs microseconds),
+// each warp's pair becomes one double, and thread 0 adds the warps' doubles in order. About 48
+// significant bits; deterministic. Result valid in the thread with flat index 0.
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+template <int NV, int NT>
+__device__ __forceinline__ void block_sum_f2(const float (&s)[NV], const float (&c)[NV], double (&val)[NV],
+                                             double* smem /* NV*NT/32 */, int tid) {
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        float hi = s[v], lo = c[v];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+            float t, e;
+            two_sum_f(hi, h2, t, e);
+            hi = t;
+            lo += l2 + e;
+        }
+        if (lane == 0) smem[v * (NT / 32) + warp] = (double)hi + (double)lo;
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            double acc = 0.0;
+            for (int w = 0; w < NT / 32; ++w) acc += smem[v * (NT / 32) + w];
+            val[v] = acc;
+        }
+    }
+}
+
 // Finishes a reduction: block `bid` of `nblocks` stores its NV partials; the last block to
 // arrive adds them and writes out[0..NV) (from thread 0). The last block sums in parallel:
 // thread t adds partials t, t+NT, t+2NT, ... in order, then a fixed tree combines the
@@ -410,6 +448,40 @@ __device__ __forceinline__ DF operator*(DF a, DF b) {
 __device__ __forceinline__ DF operator/(DF a, DF b) { return DF(a.value() / b.value()); }  // not on a hot path
 __device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
 __device__ __forceinline__ bool operator>(DF a, DF b) { return a.value() > b.value(); }
+#endif
+#ifdef __CUDACC__
+// A double as an unevaluated float pair hi + lo, by integer and FP32 operations only (FP64
+// arithmetic on this part runs at a small fraction of the FP32 rate, and a conversion per
+// value is FP64 work): hi keeps the leading 24 significant bits (truncated), lo the next 29
+// rounded to 24, so hi + lo is within 2^-48 of d. |d| below 2^-120 becomes (signed) zero and
+// |d| beyond the float range takes the FP64 path; neither occurs in the fields split here.
+__device__ __forceinline__ void split_double(double d, float& hi, float& lo) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e < 1023 - 120) {
+        hi = __uint_as_float(sign);
+        lo = 0.f;
+        return;
+    }
+    if (e > 1023 + 127) {
+        hi = (float)d;
+        lo = 0.f;
+        return;
+    }
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
+    const unsigned r = (unsigned)(m & 0x1FFFFFFFull);  // the 29 bits below hi, weight 2^(e - 1075)
+    const float scale = e > 948 ? __uint_as_float((unsigned)(e - 948) << 23) : 0.f;
+    const float l = __uint2float_rn(r) * scale;
+    lo = sign ? -l : l;
+}
+// (a_hi + a_lo) - (b_hi + b_lo) rounded to FP32
+__device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl) {
+    float s, e;
+    two_sum(ah, -bh, s, e);
+    return s + (e + (al - bl));
+}
 #endif
 struct dfpair {
     DF x, y;

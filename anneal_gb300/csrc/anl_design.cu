@@ -278,20 +278,21 @@ __device__ __forceinline__ float element_energy(const KeModal<float>& K, const d
                                                 int k) {
     const int64_t sx = 1, sy = d.nx + 1, sz = (int64_t)(d.nx + 1) * (d.ny + 1);
     const int64_t n0 = d.node(i, j, k);
-    double c[2][2][2][3];
+    // corner values as float pairs (split_double: no FP64 arithmetic), differences in
+    // double-float arithmetic rounded once to FP32
+    float ch[2][2][2][3], cl[2][2][2][3];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int px = q & 1, py = (q >> 1) & 1, pz = (q >> 2) & 1;
         const int64_t n = n0 + px * sx + py * sy + pz * sz;
-        c[px][py][pz][0] = u[3 * n];
-        c[px][py][pz][1] = u[3 * n + 1];
-        c[px][py][pz][2] = u[3 * n + 2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) split_double(__ldg(u + 3 * n + c), ch[px][py][pz][c], cl[px][py][pz][c]);
     }
     auto diff = [&](int ax, int bx, int ay, int by, int az, int bz) {
         V3<float> v;
-        v.xy.x = (float)(c[ax][ay][az][0] - c[bx][by][bz][0]);
-        v.xy.y = (float)(c[ax][ay][az][1] - c[bx][by][bz][1]);
-        v.z = (float)(c[ax][ay][az][2] - c[bx][by][bz][2]);
+        v.xy.x = df_diff(ch[ax][ay][az][0], cl[ax][ay][az][0], ch[bx][by][bz][0], cl[bx][by][bz][0]);
+        v.xy.y = df_diff(ch[ax][ay][az][1], cl[ax][ay][az][1], ch[bx][by][bz][1], cl[bx][by][bz][1]);
+        v.z = df_diff(ch[ax][ay][az][2], cl[ax][ay][az][2], ch[bx][by][bz][2], cl[bx][by][bz][2]);
         return v;
     };
     V3<float> dxb[2], dxt[2], dyb[2], dyt[2], dz[2][2];
@@ -490,9 +491,10 @@ __global__ void __launch_bounds__(DT) k_oc_vol_bank(int64_t ne, const uint8_t* _
     for (int64_t e = 4 * n4 + t; e < ne; e += stride)
         oc_bank_elem(active[e], frozen[e], x[e], dcx[e], dvx[e], wv[e], bank, rl, move, acc);
     double v[OC_BANK];
+    float zero[OC_BANK];
 #pragma unroll
-    for (int j = 0; j < OC_BANK; ++j) v[j] = acc[j];
-    block_sum<OC_BANK, DT>(v, sm, threadIdx.x);
+    for (int j = 0; j < OC_BANK; ++j) zero[j] = 0.f;
+    block_sum_f2<OC_BANK, DT>(acc, zero, v, sm, threadIdx.x);
     finish_reduction<OC_BANK, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 

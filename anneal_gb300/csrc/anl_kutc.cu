@@ -488,8 +488,9 @@ __global__ void __launch_bounds__(NT, 1) kutc_kernel(KuArgs<float> a, KeModal<fl
         tmem_dealloc(tmem, 512);
     }
     if (MODE == KU_APPLY_DOT) {
-        double v[1] = {dot.value()};
-        block_sum<1, NT>(v, sred, tid);
+        double v[1];
+        const float s1[1] = {dot.a.s}, c1[1] = {dot.a.c};
+        block_sum_f2<1, NT>(s1, c1, v, sred, tid);
         finish_reduction<1, NT>(v, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sred);
     }
 }

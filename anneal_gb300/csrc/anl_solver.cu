@@ -47,6 +47,24 @@ struct Sum<double> {
     __device__ double get() const { return s; }
 };
 
+// block sums of NV accumulators: float-pair trees for the FP32 sums, FP64 trees for FP64 ones
+template <int NV, int NT>
+__device__ __forceinline__ void block_sum_of(const Sum<float> (&acc)[NV], double (&v)[NV], double* smem, int tid) {
+    float s[NV], c[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        s[i] = acc[i].a.s;
+        c[i] = acc[i].a.c;
+    }
+    block_sum_f2<NV, NT>(s, c, v, smem, tid);
+}
+template <int NV, int NT>
+__device__ __forceinline__ void block_sum_of(const Sum<double> (&acc)[NV], double (&v)[NV], double* smem, int tid) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = acc[i].get();
+    block_sum<NV, NT>(v, smem, tid);
+}
+
 // ------------------------------------------------------------------ masks and levels
 
 __global__ void k_mask_level0(Dims d, const uint8_t* active, const uint8_t* fixed, uint8_t* nmask) {
@@ -509,10 +527,13 @@ __global__ void k_split(int64_t n, const double* x, T* hi, T* lo) {
     }
 }
 
-// x (FP64) -> (hi, lo) float pairs
+// x (FP64) -> (hi, lo) float pairs, without FP64 arithmetic (split_double)
 __global__ void k_split_df(int64_t n, const double* x, DF* xdf) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        xdf[i] = DF(x[i]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float h, l;
+        split_double(x[i], h, l);
+        xdf[i] = DF(h, l);
+    }
 }
 
 // r = b - y1 - y2 (y2 may be null), ||r||^2; sets the CG state from the true residual.
@@ -591,7 +612,9 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
     __shared__ double sm[2 * VT / 32];
     if (sc->done) return;
     const bool rs = *restart != 0;
-    Sum<T> a, b;
+    Sum<T> ab[2];
+    Sum<T>& a = ab[0];
+    Sum<T>& b = ab[1];
     for_each4(
         n,
         [&](int64_t i) {
@@ -611,8 +634,8 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
             a.prod(r[i], zi);
             if (!rs) b.prod(zi, q[i]);
         });
-    double v[2] = {a.get(), b.get()};
-    block_sum<2, VT>(v, sm, threadIdx.x);
+    double v[2];
+    block_sum_of<2, VT>(ab, v, sm, threadIdx.x);
     __shared__ double res[2];
     if (finish_reduction<2, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
         if (threadIdx.x == 0) {
@@ -669,7 +692,8 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
     const double pq = sc->pq;
     const double alpha = sc->rz[it & 1] / pq;
     const bool bad = !(pq > 0.0) || !isfinite(alpha);
-    Sum<T> rr;
+    Sum<T> rr1[1];
+    Sum<T>& rr = rr1[0];
     if (!bad) {
         const T at = T(alpha);
         for_each4(
@@ -697,8 +721,8 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
                 rr.prod(ri, ri);
             });
     }
-    double v[1] = {rr.get()};
-    block_sum<1, VT>(v, sm, threadIdx.x);
+    double v[1];
+    block_sum_of<1, VT>(rr1, v, sm, threadIdx.x);
     __shared__ double res[1];
     if (finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
         if (threadIdx.x == 0) {
