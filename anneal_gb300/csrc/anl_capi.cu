@@ -229,6 +229,8 @@ static void free_ctx(anl_ctx* c) {
     f(c->active);
     f(c->A);
     f(c->Ainv);
+    f(c->ainv_hi);
+    f(c->ainv_lo);
     f(c->flag_d);
     f(c->p);
     f(c->q);
@@ -350,6 +352,10 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     if (c->dense_coarse) {
         ALLOC(c->A, (size_t)c->nc * c->nc * sizeof(double));
         ALLOC(c->Ainv, (size_t)c->nc * c->nc * sizeof(double));
+        if (!c->fp64) {
+            ALLOC(c->ainv_hi, (size_t)c->nc * c->nc * sizeof(float));
+            ALLOC(c->ainv_lo, (size_t)c->nc * c->nc * sizeof(float));
+        }
     }
     ALLOC(c->flag_d, 4 * sizeof(int));
     ALLOC(c->cheb_d, c->lev.size() * kChebStride * sizeof(double));
@@ -401,6 +407,28 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     if (c->use_tc && kutc_prepare(c->ke) != ANL_OK) {
         free_ctx(c);
         return ANL_ERR_CUDA;
+    }
+    // the V-cycle tail: the first level (level 2 or below, on the box levels) from which every
+    // level to the coarsest fits one CTA (at most 1024 elements, the vectors in shared memory)
+    {
+        // opt-in (ANL_TAIL=1): on the 256x128x128 bench workload the one-CTA tail (levels 4-6)
+        // measured slower than the same levels as separate launches in the CUDA graph (33.2
+        // against 33.8 SIMP iterations/s, the same CG iterations)
+        const char* e = std::getenv("ANL_TAIL");
+        const bool tail_on = e && std::atoi(e) != 0;
+        const int nl = (int)c->lev.size();
+        if (tail_on && !c->fp64 && c->dense_coarse && nl >= 2) {
+            for (int l = std::max(c->box_from, 2); l <= nl - 2 && c->tail_from < 0; ++l) {
+                if (nl - l > kTailMaxLevels || c->lev[l].d.ne() > 1024) continue;
+                TailLevel tl[kTailMaxLevels];
+                for (int q = l; q < nl; ++q) tl[q - l].d = c->lev[q].d;
+                if (tail_smem_bytes(tl, nl - l) <= (size_t)kTailMaxSmem) c->tail_from = l;
+            }
+        }
+        if (c->tail_from >= 0 && vtail_prepare() != ANL_OK) {
+            free_ctx(c);
+            return ANL_ERR_CUDA;
+        }
     }
     if (cudaMallocHost((void**)&c->sc_h, sizeof(PcgScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->red_h, 16 * sizeof(double)) != cudaSuccess) {

@@ -79,6 +79,10 @@ struct anl_ctx {
     int box_from = 2;
     // the finest level's K u passes on the tensor cores (anl_kutc.cu; FP32 contexts)
     bool use_tc = false;
+    // first level of the one-CTA V-cycle tail (anl_vtail.cu; FP32 contexts), -1 for none
+    int tail_from = -1;
+    float* ainv_hi = nullptr;  // the coarsest dense inverse as float pairs (the tail's coarse solve)
+    float* ainv_lo = nullptr;
 #ifndef ANL_CHEB_LO
 #define ANL_CHEB_LO 0.03
 #endif

@@ -97,6 +97,38 @@ struct KbArgs {
 int launch_kbox(int mode, const KbArgs& a, const KeModal<float>& km, cudaStream_t s);
 void kbox_prepare();
 
+// ------------------------------------------------------------------ V-cycle tail in one CTA
+
+// The smallest levels of the V-cycle and the coarsest dense solve in one CTA (anl_vtail.cu):
+// level 0 of the tail takes b0 and returns its V-cycle correction in x0. Every level but the
+// last is smoothed (`degree` Chebyshev steps before and after); the last is solved with the
+// dense inverse as float pairs (ainv_hi + ainv_lo, nc x nc, symmetric).
+constexpr int kTailMaxLevels = 6;
+constexpr int kTailMaxSmem = 200 * 1024;
+struct TailLevel {
+    Dims d{};
+    const float* E = nullptr;
+    const uint8_t* nmask = nullptr;
+    const float* diag = nullptr;
+    const double* cheb = nullptr;  // (c1, c2) pairs of the level's sweep
+};
+struct TailArgs {
+    int nlev = 0;
+    TailLevel lev[kTailMaxLevels];
+    int degree = 0;
+    const float* b0 = nullptr;
+    float* x0 = nullptr;
+    const float* ainv_hi = nullptr;
+    const float* ainv_lo = nullptr;
+    int nc = 0;
+    const int* done = nullptr;
+    KeModal<float> km{};
+};
+size_t tail_smem_bytes(const TailLevel* lev, int nlev);
+int vtail_prepare();
+int launch_vtail(const TailArgs& a, cudaStream_t s);
+int launch_ainv_split(const double* ainv, int n, float* hi, float* lo, cudaStream_t s);
+
 // ------------------------------------------------------------------ tensor-core K u (fine grid)
 
 // The FP32 K u passes KU_APPLY, KU_APPLY_DOT, KU_RESID and KU_CHEB on the tensor cores

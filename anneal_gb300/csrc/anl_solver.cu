@@ -475,6 +475,86 @@ __global__ void __launch_bounds__(256) k_chol_inverse_smem(const double* L, doub
     for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i];
 }
 
+// The same factorisation and inverse in double-float arithmetic (about 48 bits, on the FP32
+// pipes: FP64 arithmetic on this part runs at a small fraction of FP32, and the factor's
+// trailing updates are ~n^3/6 multiply-adds on one SM). The matrix comes in as FP64 and is
+// split into float pairs without FP64 arithmetic (split_double); pivots, their square roots and
+// reciprocals (n of each) are taken in FP64. Tiny pivots are regularised as in k_cholesky.
+__device__ __forceinline__ DF df_fms(DF c, DF a, DF b) { return c - a * b; }  // c - a b
+
+__global__ void __launch_bounds__(1024) k_cholesky_df(double* A, int n, int* flag) {
+    extern __shared__ DF SD[];
+    __shared__ double piv, dmax;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        float h, l;
+        split_double(A[t], h, l);
+        SD[t] = DF(h, l);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int j = 0; j < n; ++j) m = fmax(m, SD[j * n + j].value());
+        dmax = m;
+    }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        if (threadIdx.x == 0) {
+            const double a = SD[j * n + j].value();
+            if (!(a > 1e-12 * dmax)) {
+                *flag += 1;
+                piv = sqrt(1e-12 * dmax);
+            } else {
+                piv = sqrt(a);
+            }
+            SD[j * n + j] = DF(piv);
+        }
+        __syncthreads();
+        const DF rp = DF(1.0 / piv);
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) SD[i * n + j] = SD[i * n + j] * rp;
+        __syncthreads();
+        const int m = n - j - 1;
+        for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+            const int i = j + 1 + t / m, k = j + 1 + t % m;
+            if (k <= i) SD[i * n + k] = df_fms(SD[i * n + k], SD[i * n + j], SD[k * n + j]);
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) A[t] = SD[t].value();
+}
+
+__global__ void __launch_bounds__(256) k_chol_inverse_df(const double* L, double* Ainv, int n) {
+    extern __shared__ DF SD[];  // L (n * n), reciprocal pivots (n), the column (n)
+    DF* rd = SD + n * n;
+    DF* xs = rd + n;
+    const int c = blockIdx.x;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        float h, l;
+        split_double(L[t], h, l);
+        SD[t] = DF(h, l);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        rd[i] = DF(1.0 / L[i * n + i]);
+        xs[i] = DF(i == c ? 1.f : 0.f);
+    }
+    __syncthreads();
+    for (int j = c; j < n; ++j) {  // L y = e_c (y_j = 0 for j < c)
+        const DF yj = xs[j] * rd[j];
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) xs[i] = df_fms(xs[i], SD[i * n + j], yj);
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = yj;
+        __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {  // L^T x = y
+        const DF xj = xs[j] * rd[j];
+        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] = df_fms(xs[i], SD[j * n + i], xj);
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = xj;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i].value();
+}
+
 // x = A^-1 b on the coarsest grid (FP64), one warp per row.
 template <class T>
 __global__ void k_coarse_apply(const double* Ainv, int n, const T* b, const uint8_t* nmask, T* x, const int* done) {
@@ -835,18 +915,30 @@ static int coarse_factor(anl_ctx* c, cudaStream_t s) {
                                           kCholSmemN * kCholSmemN * (int)sizeof(double)));
             ANL_CUDA(cudaFuncSetAttribute(k_chol_inverse_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (kCholSmemN * kCholSmemN + 2 * kCholSmemN) * (int)sizeof(double)));
+            ANL_CUDA(cudaFuncSetAttribute(k_cholesky_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kCholSmemN * kCholSmemN * (int)sizeof(DF)));
+            ANL_CUDA(cudaFuncSetAttribute(k_chol_inverse_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (kCholSmemN * kCholSmemN + 2 * kCholSmemN) * (int)sizeof(DF)));
             attr = true;
         }
-        k_cholesky_smem<<<1, 1024, fb, s>>>(c->A, n, c->flag_d);
-        ANL_LAUNCH_CHECK();
-        k_chol_inverse_smem<<<n, 256, ib, s>>>(c->A, c->Ainv, n);
-        ANL_LAUNCH_CHECK();
+        if (c->fp64) {
+            k_cholesky_smem<<<1, 1024, fb, s>>>(c->A, n, c->flag_d);
+            ANL_LAUNCH_CHECK();
+            k_chol_inverse_smem<<<n, 256, ib, s>>>(c->A, c->Ainv, n);
+            ANL_LAUNCH_CHECK();
+        } else {  // the FP32 solver's preconditioner: double-float factor and inverse
+            k_cholesky_df<<<1, 1024, n * n * (int)sizeof(DF), s>>>(c->A, n, c->flag_d);
+            ANL_LAUNCH_CHECK();
+            k_chol_inverse_df<<<n, 256, (n * n + 2 * n) * (int)sizeof(DF), s>>>(c->A, c->Ainv, n);
+            ANL_LAUNCH_CHECK();
+        }
     } else {
         k_cholesky<<<1, 1024, 0, s>>>(c->A, n, c->flag_d);
         ANL_LAUNCH_CHECK();
         k_chol_inverse<<<n, 128, n * sizeof(double), s>>>(c->A, c->Ainv, n);
         ANL_LAUNCH_CHECK();
     }
+    if (c->tail_from >= 0) ANL_TRY(launch_ainv_split(c->Ainv, n, c->ainv_hi, c->ainv_lo, s));
     c->coarse_ready = true;
     return ANL_OK;
 }
@@ -984,9 +1076,33 @@ static int vcycle_box(anl_ctx* c, size_t l, int deg, const int* done, cudaStream
     return ANL_OK;
 }
 
+// The levels from tail_from down in one CTA: b of level l in, its correction x out.
+static int vcycle_tail(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
+    TailArgs a;
+    a.nlev = (int)(c->lev.size() - l);
+    for (int q = 0; q < a.nlev; ++q) {
+        const Level& Lq = c->lev[l + q];
+        a.lev[q].d = Lq.d;
+        a.lev[q].E = Lq.E;
+        a.lev[q].nmask = Lq.nmask;
+        a.lev[q].diag = Lq.diag;
+        a.lev[q].cheb = c->cheb_d + (l + q) * kChebStride + 1;
+    }
+    a.degree = c->mg_degree_coarse;
+    a.b0 = (const float*)c->lev[l].b;
+    a.x0 = (float*)c->lev[l].x;
+    a.ainv_hi = c->ainv_hi;
+    a.ainv_lo = c->ainv_lo;
+    a.nc = c->nc;
+    a.done = done;
+    a.km = c->kmf;
+    return launch_vtail(a, s);
+}
+
 template <class T>
 static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     Level& L = c->lev[l];
+    if (sizeof(T) == 4 && c->tail_from >= 0 && (int)l == c->tail_from) return vcycle_tail(c, l, done, s);
     if (l + 1 == c->lev.size()) {
         if (c->dense_coarse) {
             const int n = c->nc;

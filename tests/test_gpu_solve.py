@@ -281,3 +281,25 @@ def test_box_smoother_levels_match_the_marching_kernel(monkeypatch):
     assert nlev >= 4
     assert np.abs(ub - um).max() <= 1e-6 * np.abs(um).max()
     assert abs(ib - im) <= max(2, im // 10), (ib, im)
+
+
+def test_one_cta_vcycle_tail_matches_per_level_launches(monkeypatch):
+    """The smallest multigrid levels and the coarsest solve in one CTA (ANL_TAIL=1) against the
+    same levels as separate launches: the same solution to the tolerance and about the same CG
+    iterations, on two grids (a cantilever and the L-bracket with its void)."""
+    import torch
+    for w in (P.cantilever(128, 64, 32), P.lbracket(scale=0.5, vf=0.25, r_vox=2.0, emin=1e-9)):
+        rho = P.random_density(w.shape, 9, active=w.active)
+        case = next(iter(w.loads))
+        out = {}
+        for tag, on in (("tail", "1"), ("launches", "0")):
+            monkeypatch.setenv("ANL_TAIL", on)
+            fem = G.FEM(_grid(w.shape), w.active, w.fixed, 0.3, precision="fp32")
+            Ee = 1e-9 + rho[fem.act] ** 3 * (1 - 1e-9)
+            u = fem.solve(fem.assemble(Ee), [fem.reduce_load(w.loads[case])], rtol=1e-8)[0]
+            out[tag] = (u, fem.cg_iters[-1])
+            fem.close()
+            torch.cuda.empty_cache()
+        (ut, it_t), (ul, it_l) = out["tail"], out["launches"]
+        assert np.abs(ut - ul).max() <= 1e-6 * np.abs(ul).max()
+        assert abs(it_t - it_l) <= max(2, it_l // 10), (w.name, it_t, it_l)
