@@ -21,6 +21,12 @@ ANL_ERR_STATE = 8
 ANL_ERR_STAGNATION = 9
 ANL_FLAG_FP64 = 1
 
+
+def ANL_FLAG_RHS(n):
+    """Right-hand-side slots of an FP32 context (1..255)."""
+    return int(n) << 8
+
+
 STATUS_NAMES = {0: "OK", 1: "MAXITER", 2: "NONFINITE", 3: "BREAKDOWN", 4: "BADARG", 5: "CUDA",
                 6: "SINGULAR", 7: "NOMEM", 8: "STATE", 9: "STAGNATION"}
 
@@ -35,7 +41,7 @@ EXPORTS = [
     "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
     "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam", "anl_element_stress",
     "anl_vox_create", "anl_vox_destroy", "anl_voxel_fill", "anl_output_field", "anl_choose_level",
-    "anl_label_above", "anl_edt", "anl_profile_pass",
+    "anl_label_above", "anl_edt", "anl_profile_pass", "anl_solve_status",
 ]
 
 
@@ -63,6 +69,7 @@ _SIGS = {
     "anl_free_mask": (I, [P, P, P]),
     "anl_apply_K": (I, [P, P, P, P, P]),
     "anl_solve": (I, [P, P, P, P, I, D, I, I, ctypes.POINTER(I), ctypes.POINTER(D), P]),
+    "anl_solve_status": (I, [P, I]),
     "anl_dot": (I, [P, P, P, ctypes.POINTER(D), P]),
     "anl_element_energy": (I, [P, P, P, P]),
     "anl_sensitivity": (I, [P, P, I, ctypes.POINTER(D), P, P, P, D, D, D, P, P, P]),

@@ -43,7 +43,7 @@ class Context:
     """A solver context: the grid, the free-DOF masks, the multigrid hierarchy and the
     workspaces live on the GPU until ``close()``."""
 
-    def __init__(self, shape, h=1.0, nu=0.3, fp64=False):
+    def __init__(self, shape, h=1.0, nu=0.3, fp64=False, nrhs=1):
         require_cuda()
         self.lib = N.load()
         self.shape = tuple(int(s) for s in shape)
@@ -55,9 +55,13 @@ class Context:
         self.nu = float(nu)
         self.fp64 = bool(fp64)
         self.vdtype = _F64 if fp64 else _F32
+        # right-hand-side slots: an FP32 solve of 1 < nrhs <= this many cases runs them together
+        self.nrhs = 1 if fp64 else int(nrhs)
+        if not 1 <= self.nrhs <= 255:
+            raise ValueError("nrhs must be in 1..255")
+        flags = N.ANL_FLAG_FP64 if fp64 else N.ANL_FLAG_RHS(self.nrhs)
         h_ = ctypes.c_void_p()
-        N.check(self.lib.anl_ctx_create(ctypes.byref(h_), nx, ny, nz, self.h, self.nu,
-                                        N.ANL_FLAG_FP64 if fp64 else 0), "anl_ctx_create")
+        N.check(self.lib.anl_ctx_create(ctypes.byref(h_), nx, ny, nz, self.h, self.nu, flags), "anl_ctx_create")
         self._h = h_
         self.nfree = None
         self.filter_r = None
@@ -113,6 +117,10 @@ class Context:
                       N.ANL_ERR_SINGULAR, N.ANL_ERR_STAGNATION):
             N.check(st, "anl_solve")
         return st, list(iters), list(relres)
+
+    def solve_status(self, k):
+        """Status of case k in the last solve (anl_solve returns the first non-OK one)."""
+        return int(self.lib.anl_solve_status(self._h, int(k)))
 
     def profile_apply(self, u, y, reps):
         """Mean milliseconds per launch of the level-0 K u kernel (element scales from the

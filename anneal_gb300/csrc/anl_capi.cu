@@ -209,6 +209,13 @@ static cudaError_t upload_cheb(anl_ctx* c) {
 
 static void free_ctx(anl_ctx* c) {
     if (!c) return;
+    if (c->sc_base) {  // the single-vector pointers may point at another slot: free the arrays
+        c->sc = c->sc_base;
+        c->xbuf = c->xbuf_base;
+        c->bbuf = c->bbuf_base;
+        c->bdf = c->bdf_base;
+        if (!c->lev.empty()) c->lev[0].b = c->b0_base;
+    }
     std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     auto f = [](void* p) {
         if (p) cudaFree(p);
@@ -232,6 +239,7 @@ static void free_ctx(anl_ctx* c) {
     f(c->ainv_hi);
     f(c->ainv_lo);
     f(c->flag_d);
+    f(c->restart_d);
     f(c->p);
     f(c->q);
     f(c->xhi);
@@ -271,6 +279,7 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     c->nu = nu;
     c->flags = flags;
     c->fp64 = (flags & ANL_FLAG_FP64) != 0;
+    c->rmax = std::max(1, (flags >> 8) & 0xFF);
     c->tsize = c->fp64 ? 8 : 4;
     hex8_ke(nu, 1.0, c->ke);
     const double dev = ke_blocks(c->ke, &c->kbd);
@@ -334,18 +343,21 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         dd = Dims{(dd.nx + 1) / 2, (dd.ny + 1) / 2, (dd.nz + 1) / 2};
     }
     const size_t ts = c->tsize;
+    const size_t R = (size_t)c->rmax;
     for (auto& L : c->lev) {
         const int64_t ne = L.d.ne(), nn = L.d.nn();
+        L.vs = (3 * nn + 63) / 64 * 64;
         ALLOC(L.E, ne * sizeof(float));
         ALLOC(L.eact, ne);
         ALLOC(L.nmask, nn);
         ALLOC(L.diag, nn * sizeof(float));
-        ALLOC(L.x, 3 * nn * ts);
-        ALLOC(L.xt, 3 * nn * ts);
-        ALLOC(L.b, 3 * nn * ts);
-        ALLOC(L.r, 3 * nn * ts);
-        ALLOC(L.dv, 3 * nn * ts);
+        ALLOC(L.x, R * L.vs * ts);
+        ALLOC(L.xt, R * L.vs * ts);
+        ALLOC(L.b, R * L.vs * ts);
+        ALLOC(L.r, R * L.vs * ts);
+        ALLOC(L.dv, R * L.vs * ts);
     }
+    const int64_t vs0 = c->lev[0].vs;
     const Level& C = c->lev.back();
     c->nc = (int)(3 * C.d.nn());
     c->dense_coarse = c->nc <= 700;
@@ -358,6 +370,7 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
         }
     }
     ALLOC(c->flag_d, 4 * sizeof(int));
+    ALLOC(c->restart_d, R * sizeof(int));
     ALLOC(c->cheb_d, c->lev.size() * kChebStride * sizeof(double));
     ALLOC(c->ke_d, 576 * sizeof(double));
     if (cudaMemcpy(c->ke_d, c->ke, 576 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -367,28 +380,29 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     }
     const int64_t ne = c->d.ne(), nn = c->d.nn();
     ALLOC(c->active, ne);
-    ALLOC(c->p, 3 * nn * ts);
-    ALLOC(c->q, 3 * nn * ts);
+    ALLOC(c->p, R * vs0 * ts);
+    ALLOC(c->q, R * vs0 * ts);
     ALLOC(c->xhi, 3 * nn * ts);
     ALLOC(c->xlo, 3 * nn * ts);
     if (!c->fp64) {
         ALLOC(c->xdf, 3 * nn * sizeof(DF));
-        ALLOC(c->bdf, 3 * nn * sizeof(DF));
+        ALLOC(c->bdf, R * vs0 * sizeof(DF));
     }
     ALLOC(c->y1, 3 * nn * ts);
     ALLOC(c->y2, 3 * nn * ts);
     ALLOC(c->tmp, 3 * nn * ts);
-    ALLOC(c->xbuf, 3 * nn * sizeof(double));
-    ALLOC(c->bbuf, 3 * nn * sizeof(double));
-    ALLOC(c->sc, sizeof(PcgScalars));
+    ALLOC(c->xbuf, R * vs0 * sizeof(double));
+    ALLOC(c->bbuf, R * vs0 * sizeof(double));
+    ALLOC(c->sc, R * sizeof(PcgScalars));
     c->part_cap = std::max(ku_grid_blocks(c->d), kRedBlocks);
     {
         // the filter reduction grid (32x4x2 tiles) can exceed both
         const int fb = ceil_div(c->d.nx, 32) * ceil_div(c->d.ny, 4) * ceil_div(c->d.nz, 2);
         c->part_cap = std::max(c->part_cap, fb);
     }
-    ALLOC(c->partials, (size_t)c->part_cap * kMaxRedVals * sizeof(double));
-    ALLOC(c->counter, 16 * sizeof(unsigned));
+    c->part_stride = (int64_t)c->part_cap * kMaxRedVals;
+    ALLOC(c->partials, R * c->part_stride * sizeof(double));
+    ALLOC(c->counter, (16 + R) * sizeof(unsigned));
     ALLOC(c->red_out, 16 * sizeof(double));
     ALLOC(c->filt.Hs, ne * sizeof(float));
     ALLOC(c->ftmp, ne * sizeof(float));
@@ -430,13 +444,19 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
             return ANL_ERR_CUDA;
         }
     }
-    if (cudaMallocHost((void**)&c->sc_h, sizeof(PcgScalars)) != cudaSuccess ||
+    c->b0_base = c->lev[0].b;
+    c->xbuf_base = c->xbuf;
+    c->bbuf_base = c->bbuf;
+    c->bdf_base = c->bdf;
+    c->sc_base = c->sc;
+    if (cudaMallocHost((void**)&c->sc_h, R * sizeof(PcgScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->red_h, 16 * sizeof(double)) != cudaSuccess) {
         set_error("pinned host allocation failed");
         free_ctx(c);
         return ANL_ERR_NOMEM;
     }
-    if (cudaMemset(c->counter, 0, 16 * sizeof(unsigned)) != cudaSuccess ||
+    if (cudaMemset(c->counter, 0, (16 + R) * sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(c->restart_d, 0, R * sizeof(int)) != cudaSuccess ||
         upload_cheb(c) != cudaSuccess ||
         cudaMemset(c->flag_d, 0, 4 * sizeof(int)) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
         set_error("context initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -504,6 +524,12 @@ int anl_solve(anl_ctx* ctx, const float* escale, const double* f, double* x, int
         return ANL_ERR_STATE;
     }
     return solver_solve(ctx, escale, f, x, nrhs, rtol, maxiter, rebuild, iters, relres, S(stream));
+}
+
+int anl_solve_status(const anl_ctx* ctx, int k) {
+    NEED(ctx, "anl_solve_status: null context");
+    NEED(k >= 0 && k < (int)ctx->last_status.size(), "anl_solve_status: k outside the last solve's cases");
+    return ctx->last_status[k];
 }
 
 int anl_dot(anl_ctx* ctx, const double* a, const double* b, double* out_h, anl_stream_t stream) {

@@ -22,6 +22,9 @@ struct Level {
     void* r = nullptr;        // residual scratch
     void* dv = nullptr;       // Chebyshev direction
     double lmax = 0.0;        // upper end of the smoothed spectrum of D^-1 K (diagnostics)
+    // x, xt, b, r and dv hold one vector per right-hand-side slot, vs values apart (3 nn
+    // rounded up to 64 values, so every slot starts on a 256-byte boundary)
+    int64_t vs = 0;
 };
 
 struct FilterState {
@@ -81,6 +84,23 @@ struct anl_ctx {
     bool use_tc = false;
     // first level of the one-CTA V-cycle tail (anl_vtail.cu; FP32 contexts), -1 for none
     int tail_from = -1;
+    // right-hand-side slots (ANL_FLAG_RHS): the solve's per-vector state (the hierarchy's
+    // vectors, p, q, the FP64 solution and right-hand side, its float-pair split, the PCG
+    // scalars, the restart flags, the reduction scratch) exists once per slot; a batched solve
+    // advances rb slots in lockstep, every kernel of its CG chunk taking its slot from the grid
+    int rmax = 1;
+    int rb = 1;                   // slots of the chunk being enqueued (1 outside a batched solve)
+    int slot = 0;                 // the slot the single-vector code paths work on
+    std::vector<int> last_status; // each right-hand side's status in the last anl_solve
+    int cg_rb = 0;                // slots of the captured CG chunk
+    int64_t part_stride = 0;      // doubles of reduction scratch per slot
+    int* restart_d = nullptr;     // per-slot restart flags (p = z on the next direction update)
+    // slot 0 of the per-slot arrays (the single-vector code paths point at one slot at a time)
+    void* b0_base = nullptr;
+    double* xbuf_base = nullptr;
+    double* bbuf_base = nullptr;
+    void* bdf_base = nullptr;
+    anl::PcgScalars* sc_base = nullptr;
     float* ainv_hi = nullptr;  // the coarsest dense inverse as float pairs (the tail's coarse solve)
     float* ainv_lo = nullptr;
 #ifndef ANL_CHEB_LO

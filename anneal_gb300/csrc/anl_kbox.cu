@@ -51,6 +51,16 @@ __host__ __device__ constexpr int boxes(int nodes) { return (nodes + BO - 1) / B
 
 template <int MODE>
 __global__ void __launch_bounds__(BT) kbox_kernel(KbArgs a, KeModal<float> km) {
+    if (blockIdx.y > 0) {  // batch slot r of a multi-right-hand-side launch
+        const int r = blockIdx.y;
+        a.u = slot_ptr(a.u, r, a.vstride);
+        a.b = slot_ptr(a.b, r, a.vstride);
+        a.y = slot_ptr(a.y, r, a.vstride);
+        a.dv = slot_ptr(a.dv, r, a.vstride);
+        a.xout = slot_ptr(a.xout, r, a.vstride);
+        a.xc = slot_ptr(a.xc, r, a.cstride);
+        a.done = slot_bytes(a.done, r, a.sc_bytes);
+    }
     if (a.done != nullptr && *a.done) return;
     extern __shared__ __align__(16) float kb_smem[];
     float* su = kb_smem + OFF_U;
@@ -256,7 +266,7 @@ int launch_kbox(int mode, const KbArgs& a, const KeModal<float>& km, cudaStream_
         set_error("box smoother: grid %d x %d x %d too large", a.d.nx, a.d.ny, a.d.nz);
         return ANL_ERR_BADARG;
     }
-    const dim3 grid((unsigned)nb), block(BT);
+    const dim3 grid((unsigned)nb, (unsigned)std::max(1, a.nrhs)), block(BT);
     switch (mode) {
         case KB_RESID: kbox_kernel<KB_RESID><<<grid, block, SMEM_BYTES, s>>>(a, km); break;
         case KB_CHEB: kbox_kernel<KB_CHEB><<<grid, block, SMEM_BYTES, s>>>(a, km); break;

@@ -1,6 +1,8 @@
 // anl_kernels.cuh -- launch interfaces shared by the translation units of the library.
 #pragma once
 
+#include <type_traits>
+
 #include "anl_common.cuh"
 
 namespace anl {
@@ -58,7 +60,40 @@ struct KuArgs {
     int partial_capacity = 0;
     double* red_out = nullptr;       // APPLY_DOT: u . K u
     const int* done = nullptr;       // early-exit flag of the CG loop (may be null)
+    // batch of right-hand sides (grid.y): slot r reads and writes its nodal vectors at
+    // + r * vstride values, its done flag and dot at + r * sc_bytes bytes, its reduction scratch
+    // at partials + r * part_stride and counter + r
+    int nrhs = 1;
+    int64_t vstride = 0;
+    int sc_bytes = 0;
+    int64_t part_stride = 0;
 };
+
+// The slot of a batched launch: offsets a pointer by `r` strides (elements) or bytes.
+template <class P>
+__host__ __device__ __forceinline__ P* slot_ptr(P* p, int r, int64_t stride) {
+    return p ? p + (int64_t)r * stride : p;
+}
+template <class P>
+__host__ __device__ __forceinline__ P* slot_bytes(P* p, int r, int bytes) {
+    return p ? reinterpret_cast<P*>(reinterpret_cast<typename std::conditional<std::is_const<P>::value, const char*, char*>::type>(p) +
+                                    (int64_t)r * bytes)
+             : p;
+}
+// A K u argument block moved to batch slot r (the element fields and masks are shared).
+template <class T>
+__host__ __device__ __forceinline__ void ku_to_slot(KuArgs<T>& a, int r) {
+    if (r == 0) return;
+    a.u = slot_ptr(a.u, r, a.vstride);
+    a.y = slot_ptr(a.y, r, a.vstride);
+    a.b = slot_ptr(a.b, r, a.vstride);
+    a.dv = slot_ptr(a.dv, r, a.vstride);
+    a.xout = slot_ptr(a.xout, r, a.vstride);
+    a.done = slot_bytes(a.done, r, a.sc_bytes);
+    a.red_out = slot_bytes(a.red_out, r, a.sc_bytes);
+    a.partials = slot_ptr(a.partials, r, a.part_stride);
+    a.counter = slot_ptr(a.counter, r, (int64_t)1);
+}
 
 template <class T>
 int launch_ku(int mode, const KuArgs<T>& a, const KeModal<T>& km, cudaStream_t s);
@@ -92,6 +127,11 @@ struct KbArgs {
     Dims dc{};                       // KB_PCHEB: the coarse level and its correction
     const float* xc = nullptr;
     const int* done = nullptr;       // early-exit flag of the CG loop (may be null)
+    // batch of right-hand sides (grid.y), as in KuArgs; cstride: the coarse correction's slot stride
+    int nrhs = 1;
+    int64_t vstride = 0;
+    int64_t cstride = 0;
+    int sc_bytes = 0;
 };
 
 int launch_kbox(int mode, const KbArgs& a, const KeModal<float>& km, cudaStream_t s);

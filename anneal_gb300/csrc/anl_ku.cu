@@ -400,6 +400,7 @@ __global__ void __launch_bounds__(KmCfg<T>::NT, KmCfg<T>::MINB) ku_kernel(KuArgs
     extern __shared__ __align__(16) unsigned char ku_smem_raw[];
     auto& sm = *reinterpret_cast<typename Tile::Smem*>(ku_smem_raw);
     __shared__ double sred[NT / 32];
+    ku_to_slot(a, blockIdx.y);
     if (a.done != nullptr && *a.done) return;
 
     Tile t(a, km, sm);
@@ -500,21 +501,24 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
         case KU_CHEB0: resident = ku_resident<T, KU_CHEB0>(); break;
         default: return ANL_ERR_BADARG;
     }
-    // one wave of CTAs. A segment costs one extra element layer, but a plane step is a
-    // ~1 us latency chain, so small (coarse-level) grids spread over many short segments.
-    a.kz = (int)std::max<int64_t>(2, (total + resident - 1) / resident);
+    // one wave of CTAs (shared by the batch's right-hand sides). A segment costs one extra
+    // element layer, but a plane step is a ~1 us latency chain, so small (coarse-level) grids
+    // spread over many short segments.
+    const int per_rhs = std::max(1, resident / std::max(1, a.nrhs));
+    a.kz = (int)std::max<int64_t>(2, (total + per_rhs - 1) / per_rhs);
     const int blocks = (int)((total + a.kz - 1) / a.kz);
     dim3 block(32, KmCfg<T>::NW);
+    const dim3 grid(blocks, std::max(1, a.nrhs));
     if (mode == KU_APPLY_DOT && blocks > a.partial_capacity) {
         set_error("K u dot: %d blocks exceed the reduction scratch (%d)", blocks, a.partial_capacity);
         return ANL_ERR_BADARG;
     }
     switch (mode) {
-        case KU_APPLY: ku_kernel<T, KU_APPLY><<<blocks, block, sizeof(KuSmem<T, KU_APPLY>), s>>>(a, km); break;
-        case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<blocks, block, sizeof(KuSmem<T, KU_APPLY_DOT>), s>>>(a, km); break;
-        case KU_RESID: ku_kernel<T, KU_RESID><<<blocks, block, sizeof(KuSmem<T, KU_RESID>), s>>>(a, km); break;
-        case KU_CHEB: ku_kernel<T, KU_CHEB><<<blocks, block, sizeof(KuSmem<T, KU_CHEB>), s>>>(a, km); break;
-        case KU_CHEB0: ku_kernel<T, KU_CHEB0><<<blocks, block, sizeof(KuSmem<T, KU_CHEB0>), s>>>(a, km); break;
+        case KU_APPLY: ku_kernel<T, KU_APPLY><<<grid, block, sizeof(KuSmem<T, KU_APPLY>), s>>>(a, km); break;
+        case KU_APPLY_DOT: ku_kernel<T, KU_APPLY_DOT><<<grid, block, sizeof(KuSmem<T, KU_APPLY_DOT>), s>>>(a, km); break;
+        case KU_RESID: ku_kernel<T, KU_RESID><<<grid, block, sizeof(KuSmem<T, KU_RESID>), s>>>(a, km); break;
+        case KU_CHEB: ku_kernel<T, KU_CHEB><<<grid, block, sizeof(KuSmem<T, KU_CHEB>), s>>>(a, km); break;
+        case KU_CHEB0: ku_kernel<T, KU_CHEB0><<<grid, block, sizeof(KuSmem<T, KU_CHEB0>), s>>>(a, km); break;
         default: return ANL_ERR_BADARG;
     }
     ANL_LAUNCH_CHECK();

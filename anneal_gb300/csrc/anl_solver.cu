@@ -177,18 +177,34 @@ __global__ void k_diag(Dims d, const float* E, float kdiag, float* diag /* 1 / d
 // Grid transfers run one thread per output node on a 3-D launch (32 x 4 threads over x and y,
 // one z plane per block row), so no thread divides a flat index: at the finest level the
 // transfers are bound by their reads and writes.
+// A batch of right-hand sides in one launch: slot r's vectors sit r * fs (this level, or the
+// fine level of a transfer) or r * cs (the coarse level of a transfer) values after slot 0's,
+// its PCG scalars (done flag) r * sc_bytes bytes after, its reduction scratch r * ps doubles
+// after (and its ticket counter r after). nrhs = 1 is the plain single-vector launch.
+struct Bt {
+    int nrhs = 1;
+    int64_t fs = 0, cs = 0;
+    int sc_bytes = 0;
+    int64_t ps = 0;
+};
+
 constexpr int TR_X = 32, TR_Y = 4;
-static inline dim3 transfer_grid(const Dims& d) {
-    return dim3((unsigned)((d.nx + 1 + TR_X - 1) / TR_X), (unsigned)((d.ny + 1 + TR_Y - 1) / TR_Y), (unsigned)(d.nz + 1));
+static inline dim3 transfer_grid(const Dims& d, int nrhs = 1) {
+    return dim3((unsigned)((d.nx + 1 + TR_X - 1) / TR_X), (unsigned)((d.ny + 1 + TR_Y - 1) / TR_Y),
+                (unsigned)((d.nz + 1) * nrhs));
 }
 
 // b_c = R r_f = P^T r_f (trilinear weights 1, 1/2, 1/4, 1/8), zero on fixed coarse DOFs
 template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const T* __restrict__ rf,
                                                           const uint8_t* __restrict__ nmc, T* __restrict__ bc,
-                                                          const int* done) {
+                                                          const int* done, Bt bt) {
+    const int slot = blockIdx.z / (c.nz + 1), K = blockIdx.z - slot * (c.nz + 1);
+    rf = slot_ptr(rf, slot, bt.fs);
+    bc = slot_ptr(bc, slot, bt.cs);
+    done = slot_bytes(done, slot, bt.sc_bytes);
     if (done && *done) return;
-    const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y, K = blockIdx.z;
+    const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y;
     if (I > c.nx || J > c.ny) return;
     const int64_t fx = f.nx + 1, fxy = fx * (f.ny + 1);
     T acc0 = T(0), acc1 = T(0), acc2 = T(0);
@@ -230,9 +246,13 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
 template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
                                                                 const uint8_t* __restrict__ nmf, T* __restrict__ xf,
-                                                                const int* done) {
+                                                                const int* done, Bt bt) {
+    const int slot = blockIdx.z / (c.nz + 1), K = blockIdx.z - slot * (c.nz + 1);
+    xc = slot_ptr(xc, slot, bt.cs);
+    xf = slot_ptr(xf, slot, bt.fs);
+    done = slot_bytes(done, slot, bt.sc_bytes);
     if (done && *done) return;
-    const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y, K = blockIdx.z;
+    const int I = blockIdx.x * TR_X + threadIdx.x, J = blockIdx.y * TR_Y + threadIdx.y;
     if (I > c.nx || J > c.ny) return;
     const int64_t cx = c.nx + 1, cxy = cx * (c.ny + 1);
     const int64_t fx = f.nx + 1, fxy = fx * (f.ny + 1);
@@ -292,7 +312,11 @@ __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, 
 // x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
 template <class T>
 __global__ void k_cheb_first(int64_t nn, const T* b, const float* dinv, const uint8_t* nmask, const double* c2p, T* x,
-                             T* dv, const int* done) {
+                             T* dv, const int* done, Bt bt) {
+    b = slot_ptr(b, blockIdx.y, bt.fs);
+    x = slot_ptr(x, blockIdx.y, bt.fs);
+    dv = slot_ptr(dv, blockIdx.y, bt.fs);
+    done = slot_bytes(done, blockIdx.y, bt.sc_bytes);
     if (done && *done) return;
     const T c2 = T(*c2p);
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn; n += (int64_t)gridDim.x * blockDim.x) {
@@ -557,7 +581,11 @@ __global__ void __launch_bounds__(256) k_chol_inverse_df(const double* L, double
 
 // x = A^-1 b on the coarsest grid (FP64), one warp per row.
 template <class T>
-__global__ void k_coarse_apply(const double* Ainv, int n, const T* b, const uint8_t* nmask, T* x, const int* done) {
+__global__ void k_coarse_apply(const double* Ainv, int n, const T* b, const uint8_t* nmask, T* x, const int* done,
+                               Bt bt) {
+    b = slot_ptr(b, blockIdx.y, bt.fs);
+    x = slot_ptr(x, blockIdx.y, bt.fs);
+    done = slot_bytes(done, blockIdx.y, bt.sc_bytes);
     if (done && *done) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -688,8 +716,18 @@ __device__ __forceinline__ void for_each4(int64_t n, F4 f4, F1 f1) {
 
 template <class T>
 __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgScalars* sc, const int* restart,
-                             double* partials, unsigned* counter) {
+                             double* partials, unsigned* counter, Bt bt) {
     __shared__ double sm[2 * VT / 32];
+    {  // batch slot (grid.y)
+        const int sl = blockIdx.y;
+        r = slot_ptr(r, sl, bt.fs);
+        z = slot_ptr(z, sl, bt.fs);
+        q = slot_ptr(q, sl, bt.fs);
+        sc += sl;
+        restart += sl;
+        partials = slot_ptr(partials, sl, bt.ps);
+        counter += sl;
+    }
     if (sc->done) return;
     const bool rs = *restart != 0;
     Sum<T> ab[2];
@@ -733,7 +771,11 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
 }
 
 template <class T>
-__global__ void k_pupdate(int64_t n, const T* z, T* p, const PcgScalars* sc, const int* restart) {
+__global__ void k_pupdate(int64_t n, const T* z, T* p, const PcgScalars* sc, const int* restart, Bt batch) {
+    z = slot_ptr(z, blockIdx.y, batch.fs);
+    p = slot_ptr(p, blockIdx.y, batch.fs);
+    sc += blockIdx.y;
+    restart += blockIdx.y;
     if (sc->done) return;
     const int it = sc->iters;
     if (*restart) {  // p = z (not z + 0 p: p may hold non-finite values after a breakdown)
@@ -765,8 +807,19 @@ constexpr double kRecurrenceMargin = 0.5;  // (0.71 rtol)^2: the recurrence targ
 
 template <class T>
 __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgScalars* sc, int* restart,
-                       double* partials, unsigned* counter) {
+                       double* partials, unsigned* counter, Bt bt) {
     __shared__ double sm[VT / 32];
+    {  // batch slot (grid.y)
+        const int sl = blockIdx.y;
+        p = slot_ptr(p, sl, bt.fs);
+        q = slot_ptr(q, sl, bt.fs);
+        x = slot_ptr(x, sl, bt.fs);
+        r = slot_ptr(r, sl, bt.fs);
+        sc += sl;
+        restart += sl;
+        partials = slot_ptr(partials, sl, bt.ps);
+        counter += sl;
+    }
     if (sc->done) return;
     const int it = sc->iters;
     const double pq = sc->pq;
@@ -845,7 +898,7 @@ KeModal<double> modal_of<double>(const anl_ctx* c) { return c->kmd; }
 template <class T>
 static int ku_pass(anl_ctx* c, const Level& L, int mode, const KuArgs<T>& a, cudaStream_t s) {
     if constexpr (sizeof(T) == 4) {
-        if (c->use_tc && &L == &c->lev[0]) {
+        if (c->use_tc && c->rb == 1 && &L == &c->lev[0]) {
             KuArgs<float> t = a;
             t.diag = L.diag;
             return launch_kutc(mode, t, c->kmf, s);
@@ -864,7 +917,34 @@ static KuArgs<T> ku_args(anl_ctx* c, const Level& L) {
     a.partials = c->partials;
     a.counter = c->counter;
     a.partial_capacity = c->part_cap;
+    a.nrhs = c->rb;
+    a.vstride = L.vs;
+    a.sc_bytes = (int)sizeof(PcgScalars);
+    a.part_stride = c->part_stride;
     return a;
+}
+
+// the batch descriptor of a launch on level L (and its coarse level C for transfers)
+static Bt bt_of(const anl_ctx* c, const Level& L, const Level* C = nullptr) {
+    Bt b;
+    b.nrhs = c->rb;
+    b.fs = L.vs;
+    b.cs = C ? C->vs : 0;
+    b.sc_bytes = (int)sizeof(PcgScalars);
+    b.ps = c->part_stride;
+    return b;
+}
+
+// Points the single-vector state (level-0 right-hand side / residual, the FP64 solution and
+// right-hand side, the float-pair right-hand side, the PCG scalars, the restart flag) at slot r.
+static void set_slot(anl_ctx* c, int r) {
+    c->slot = r;
+    const int64_t vs0 = c->lev[0].vs;
+    c->lev[0].b = (char*)c->b0_base + (size_t)r * vs0 * c->tsize;
+    c->xbuf = c->xbuf_base + (size_t)r * vs0;
+    c->bbuf = c->bbuf_base + (size_t)r * vs0;
+    if (c->bdf_base) c->bdf = (DF*)c->bdf_base + (size_t)r * vs0;
+    c->sc = c->sc_base + r;
 }
 
 template <class T>
@@ -984,8 +1064,8 @@ static int smooth(anl_ctx* c, Level& L, int degree, bool x_is_zero, const int* d
         ANL_TRY(launch_ku<T>(KU_CHEB0, a, modal_of<T>(c), s));
         k0 = 2;
     } else if (x_is_zero) {
-        k_cheb_first<T><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const T*)L.b, L.diag, L.nmask, cf + 1, (T*)L.x,
-                                                         (T*)L.dv, done);
+        k_cheb_first<T><<<dim3(vgrid(L.d.nn()), c->rb), VT, 0, s>>>(L.d.nn(), (const T*)L.b, L.diag, L.nmask, cf + 1,
+                                                                     (T*)L.x, (T*)L.dv, done, bt_of(c, L));
         ANL_LAUNCH_CHECK();
         k0 = 1;
     }
@@ -1022,6 +1102,10 @@ static int vcycle_box(anl_ctx* c, size_t l, int deg, const int* done, cudaStream
     base.diag = L.diag;
     base.b = (const float*)L.b;
     base.done = done;
+    base.nrhs = c->rb;
+    base.vstride = L.vs;
+    base.cstride = C.vs;
+    base.sc_bytes = (int)sizeof(PcgScalars);
     int k0 = 0;
     if (deg >= 2) {
         KbArgs a = base;
@@ -1033,8 +1117,8 @@ static int vcycle_box(anl_ctx* c, size_t l, int deg, const int* done, cudaStream
         ANL_TRY(launch_kbox(KB_CHEB0, a, c->kmf, s));
         k0 = 2;
     } else {
-        k_cheb_first<float><<<vgrid(L.d.nn()), VT, 0, s>>>(L.d.nn(), (const float*)L.b, L.diag, L.nmask, cf + 1,
-                                                            (float*)L.x, (float*)L.dv, done);
+        k_cheb_first<float><<<dim3(vgrid(L.d.nn()), c->rb), VT, 0, s>>>(L.d.nn(), (const float*)L.b, L.diag, L.nmask, cf + 1,
+                                                            (float*)L.x, (float*)L.dv, done, bt_of(c, L));
         ANL_LAUNCH_CHECK();
         k0 = 1;
     }
@@ -1054,8 +1138,8 @@ static int vcycle_box(anl_ctx* c, size_t l, int deg, const int* done, cudaStream
         a.y = (float*)L.r;
         ANL_TRY(launch_kbox(KB_RESID, a, c->kmf, s));
     }
-    k_restrict<float><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const float*)L.r, C.nmask,
-                                                                     (float*)C.b, done);
+    k_restrict<float><<<transfer_grid(C.d, c->rb), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const float*)L.r, C.nmask,
+                                                                            (float*)C.b, done, bt_of(c, L, &C));
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<float>(c, l + 1, done, s));
     for (int k = 0; k < deg; ++k) {
@@ -1102,12 +1186,12 @@ static int vcycle_tail(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
 template <class T>
 static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     Level& L = c->lev[l];
-    if (sizeof(T) == 4 && c->tail_from >= 0 && (int)l == c->tail_from) return vcycle_tail(c, l, done, s);
+    if (sizeof(T) == 4 && c->rb == 1 && c->tail_from >= 0 && (int)l == c->tail_from) return vcycle_tail(c, l, done, s);
     if (l + 1 == c->lev.size()) {
         if (c->dense_coarse) {
             const int n = c->nc;
-            k_coarse_apply<T><<<std::max(1, (n * 32 + 255) / 256), 256, 0, s>>>(c->Ainv, n, (const T*)L.b, L.nmask,
-                                                                             (T*)L.x, done);
+            k_coarse_apply<T><<<dim3(std::max(1, (n * 32 + 255) / 256), c->rb), 256, 0, s>>>(
+                c->Ainv, n, (const T*)L.b, L.nmask, (T*)L.x, done, bt_of(c, L));
             ANL_LAUNCH_CHECK();
             return ANL_OK;
         }
@@ -1123,10 +1207,12 @@ static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     a.y = (T*)L.r;
     a.done = done;
     ANL_TRY(ku_pass<T>(c, L, KU_RESID, a, s));
-    k_restrict<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done);
+    k_restrict<T><<<transfer_grid(C.d, c->rb), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)L.r, C.nmask, (T*)C.b, done,
+                                                                        bt_of(c, L, &C));
     ANL_LAUNCH_CHECK();
     ANL_TRY(vcycle<T>(c, l + 1, done, s));
-    k_prolong_add<T><<<transfer_grid(C.d), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x, done);
+    k_prolong_add<T><<<transfer_grid(C.d, c->rb), dim3(TR_X, TR_Y), 0, s>>>(L.d, C.d, (const T*)C.x, L.nmask, (T*)L.x,
+                                                                            done, bt_of(c, L, &C));
     ANL_LAUNCH_CHECK();
     ANL_TRY(smooth<T>(c, L, deg, false, done, s));
     return ANL_OK;
@@ -1200,19 +1286,21 @@ template <class T>
 static int enqueue_chunk(anl_ctx* c, int chunk, cudaStream_t s) {
     Level& L0 = c->lev[0];
     const int64_t n = 3 * L0.d.nn();
-    int* restart = c->flag_d + 1;
+    int* restart = c->restart_d + c->slot;
     const int* done = &c->sc->done;
+    const Bt bt = bt_of(c, L0);
+    const dim3 vg(vgrid(n), c->rb);
     for (int k = 0; k < chunk; ++k) {
         ANL_TRY(vcycle<T>(c, 0, done, s));
         const T* z = (const T*)L0.x;
-        k_dots_rz_zq<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)L0.b, z, (const T*)c->q, c->sc, restart, c->partials,
-                                                 c->counter);
+        k_dots_rz_zq<T><<<vg, VT, 0, s>>>(n, (const T*)L0.b, z, (const T*)c->q, c->sc, restart, c->partials,
+                                           c->counter, bt);
         ANL_LAUNCH_CHECK();
-        k_pupdate<T><<<vgrid(n), VT, 0, s>>>(n, z, (T*)c->p, c->sc, restart);
+        k_pupdate<T><<<vg, VT, 0, s>>>(n, z, (T*)c->p, c->sc, restart, bt);
         ANL_LAUNCH_CHECK();
         ANL_TRY(apply_level<T>(c, L0, (const T*)c->p, (T*)c->q, s, &c->sc->pq, done));
-        k_axpy<T><<<vgrid(n), VT, 0, s>>>(n, (const T*)c->p, (const T*)c->q, c->xbuf, (T*)L0.b, c->sc, restart,
-                                          c->partials, c->counter);
+        k_axpy<T><<<vg, VT, 0, s>>>(n, (const T*)c->p, (const T*)c->q, c->xbuf, (T*)L0.b, c->sc, restart,
+                                    c->partials, c->counter, bt);
         ANL_LAUNCH_CHECK();
     }
     return ANL_OK;
@@ -1252,6 +1340,7 @@ static int capture_chunk(anl_ctx* c, int chunk) {
     }
     c->cg_nodes = (int)nodes;
     c->cg_valid = true;
+    c->cg_rb = c->rb;
     return ANL_OK;
 }
 
@@ -1260,7 +1349,7 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
                    cudaStream_t s) {
     Level& L0 = c->lev[0];
     const int64_t nn = L0.d.nn(), n = 3 * nn;
-    int* restart = c->flag_d + 1;
+    int* restart = c->restart_d + c->slot;
     k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, f, L0.nmask, c->bbuf);
     ANL_LAUNCH_CHECK();
     k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, x, L0.nmask, c->xbuf);
@@ -1299,7 +1388,7 @@ static int pcg_one(anl_ctx* c, const double* f, double* x, double rtol, int maxi
     while (c->sc_h->done != 1) {
         if (c->sc_h->done == 0) {
             if (c->use_graph) {
-                if (!c->cg_valid) ANL_TRY(capture_chunk<T>(c, chunk));
+                if (!c->cg_valid || c->cg_rb != c->rb) ANL_TRY(capture_chunk<T>(c, chunk));
                 ANL_CUDA(cudaGraphLaunch(c->cg_exec, s));
                 count_launches(c->cg_nodes);
             } else {
@@ -1430,6 +1519,164 @@ int solver_apply(anl_ctx* c, const float* escale, const void* u, void* y, cudaSt
     return apply_level<float>(c, L0, (const float*)c->tmp, (float*)y, s);
 }
 
+// The R right-hand sides of a batch (FP32 contexts, R <= rmax) solved together: every kernel of
+// the CG chunk (the V-cycle on all levels, the dot products, the direction and solution updates,
+// q = K p) runs once for all slots, each slot with its own FP64 scalars, so one captured graph
+// advances all of them in lockstep and a converged slot's kernels return at once. The
+// per-slot steps outside the chunk (set-up, residual replacements, certification on the FP64
+// operator's accurate residual, the acceptance rules) are those of pcg_one, slot by slot.
+// statuses[r] receives each slot's status.
+template <class T>
+static int pcg_batch(anl_ctx* c, int R, const double* f, double* x, double rtol, int maxiter, int* iters,
+                     double* relres, int* statuses, cudaStream_t s) {
+    Level& L0 = c->lev[0];
+    const int64_t nn = L0.d.nn(), n = 3 * nn;
+    const int one = 1;
+    struct SlotState {
+        bool active = true;
+        int last_replace = 0;
+        double rr_replace = 0.0, stag_ref = -1.0;
+        int status = ANL_OK;
+    };
+    std::vector<SlotState> st(R);
+    for (int r = 0; r < R; ++r) {  // set-up, as pcg_one
+        set_slot(c, r);
+        k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, f + r * n, L0.nmask, c->bbuf);
+        ANL_LAUNCH_CHECK();
+        k_mask_copy_d<<<vgrid(nn), VT, 0, s>>>(nn, x + r * n, L0.nmask, c->xbuf);
+        ANL_LAUNCH_CHECK();
+        k_split_df<<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (DF*)c->bdf);
+        ANL_LAUNCH_CHECK();
+        k_dot_d<<<vgrid(n), VT, 0, s>>>(n, c->bbuf, c->bbuf, c->partials, c->counter, c->red_out);
+        ANL_LAUNCH_CHECK();
+        k_init_scalars<<<1, 1, 0, s>>>(c->sc, rtol, maxiter, c->red_out);
+        ANL_LAUNCH_CHECK();
+        ANL_TRY(true_residual<T>(c, 1, s, false));
+        ANL_CUDA(cudaMemcpyAsync(c->restart_d + r, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    set_slot(c, 0);
+    auto fetch = [&](int r) -> int {  // host copy of slot r's scalars
+        ANL_CUDA(cudaMemcpyAsync(c->sc_h + r, c->sc_base + r, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+        ANL_CUDA(cudaStreamSynchronize(s));
+        return ANL_OK;
+    };
+    auto finish = [&](int r, int status) -> int {  // slot r leaves the batch: its kernels stop
+        st[r].active = false;
+        st[r].status = status;
+        const int stop = 5;
+        ANL_CUDA(cudaMemcpyAsync(&c->sc_base[r].done, &stop, sizeof(int), cudaMemcpyHostToDevice, s));
+        return ANL_OK;
+    };
+    ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc_base, R * sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    for (int r = 0; r < R; ++r) {
+        PcgScalars& h = c->sc_h[r];
+        if (h.bb == 0.0) {  // zero load: zero solution
+            ANL_CUDA(cudaMemsetAsync(c->xbuf_base + r * L0.vs, 0, n * sizeof(double), s));
+            ANL_TRY(finish(r, ANL_OK));
+            continue;
+        }
+        if (h.done == 1) {  // certify an already-converged initial guess
+            set_slot(c, r);
+            ANL_TRY(true_residual<T>(c, 1, s, true));
+            set_slot(c, 0);
+            ANL_TRY(fetch(r));
+            if (c->sc_h[r].done == 1) ANL_TRY(finish(r, ANL_OK));
+        }
+        st[r].rr_replace = c->sc_h[r].rr;
+    }
+    const int chunk = 4;  // even: the V-cycle buffer swaps return to their start (graph replay)
+    while (true) {
+        bool any_active = false, any_running = false;
+        for (int r = 0; r < R; ++r)
+            if (st[r].active) {
+                any_active = true;
+                any_running |= c->sc_h[r].done == 0;
+            }
+        if (!any_active) break;
+        if (any_running) {
+            c->rb = R;
+            int e;
+            if (c->use_graph) {
+                e = ANL_OK;
+                if (!c->cg_valid || c->cg_rb != c->rb) e = capture_chunk<T>(c, chunk);
+                if (e == ANL_OK) {
+                    const cudaError_t ce = cudaGraphLaunch(c->cg_exec, s);
+                    if (ce != cudaSuccess) {
+                        set_error("CG graph launch failed: %s", cudaGetErrorString(ce));
+                        e = ANL_ERR_CUDA;
+                    }
+                    count_launches(c->cg_nodes);
+                }
+            } else {
+                e = enqueue_chunk<T>(c, chunk, s);
+            }
+            c->rb = 1;
+            ANL_TRY(e);
+            ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc_base, R * sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+            ANL_CUDA(cudaStreamSynchronize(s));
+        }
+        for (int r = 0; r < R; ++r) {
+            if (!st[r].active) continue;
+            const PcgScalars h = c->sc_h[r];
+            if (h.done == 3) {
+                ANL_TRY(finish(r, ANL_ERR_NONFINITE));
+                continue;
+            }
+            const bool want_check = h.done == 1 || h.done == 2 || h.done == 4 || h.iters - st[r].last_replace >= 50 ||
+                                    (h.rr <= 1e-6 * st[r].rr_replace && h.rr > 100.0 * h.tol2);
+            if (!want_check) continue;
+            set_slot(c, r);
+            ANL_TRY(true_residual<T>(c, 1, s, true));
+            set_slot(c, 0);
+            ANL_TRY(fetch(r));
+            const PcgScalars& t = c->sc_h[r];
+            st[r].last_replace = t.iters;
+            st[r].rr_replace = t.rr_true;
+            if (t.done == 1) {
+                st[r].active = false;  // certified (done stays 1: its kernels return)
+                continue;
+            }
+            if (t.done == 3) {
+                ANL_TRY(finish(r, ANL_ERR_NONFINITE));
+                continue;
+            }
+            const double floor2 = std::max(1e4 * t.tol2, 1e-20 * t.bb);
+            if (h.done == 1 || h.done == 4) {
+                const bool stalled = st[r].stag_ref > 0 && t.rr_true >= 0.25 * st[r].stag_ref;
+                if (stalled && sizeof(T) == 4) {
+                    ANL_TRY(finish(r, ANL_ERR_STAGNATION));
+                    continue;
+                }
+                if (stalled && t.rr_true <= floor2) {
+                    ANL_TRY(finish(r, ANL_OK));
+                    continue;
+                }
+                if (st[r].stag_ref < 0 || t.rr_true < st[r].stag_ref) st[r].stag_ref = t.rr_true;
+                if (h.done == 4 && t.rr_true > floor2) {
+                    ANL_TRY(finish(r, ANL_ERR_BREAKDOWN));
+                    continue;
+                }
+            }
+            if (t.iters >= maxiter) {
+                ANL_TRY(finish(r, ANL_ERR_MAXITER));
+                continue;
+            }
+            if (h.done == 4) ANL_CUDA(cudaMemcpyAsync(c->restart_d + r, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+        }
+    }
+    ANL_CUDA(cudaMemcpyAsync(c->sc_h, c->sc_base, R * sizeof(PcgScalars), cudaMemcpyDeviceToHost, s));
+    ANL_CUDA(cudaStreamSynchronize(s));
+    for (int r = 0; r < R; ++r) {
+        const PcgScalars& h = c->sc_h[r];
+        iters[r] = h.iters;
+        relres[r] = h.bb > 0 ? std::sqrt(std::max(h.rr_true, 0.0) / h.bb) : 0.0;
+        statuses[r] = st[r].status;
+        ANL_CUDA(cudaMemcpyAsync(x + r * n, c->xbuf_base + r * L0.vs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    return ANL_OK;
+}
+
 int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, int nrhs, double rtol, int maxiter,
                  int rebuild, int* iters, double* relres, cudaStream_t s) {
     ANL_TRY(solver_set_escale(c, escale, s));
@@ -1437,11 +1684,22 @@ int solver_solve(anl_ctx* c, const float* escale, const double* f, double* x, in
     else ANL_TRY(update_hierarchy<float>(c, rebuild != 0, s));
     const int64_t n = 3 * c->lev[0].d.nn();
     int worst = ANL_OK;
-    for (int k = 0; k < nrhs; ++k) {
-        int st = c->fp64 ? pcg_one<double>(c, f + k * n, x + k * n, rtol, maxiter, iters + k, relres + k, s)
-                         : pcg_one<float>(c, f + k * n, x + k * n, rtol, maxiter, iters + k, relres + k, s);
-        if (st == ANL_ERR_CUDA) return st;
-        if (st != ANL_OK && worst == ANL_OK) worst = st;
+    set_slot(c, 0);
+    if (!c->fp64 && nrhs > 1 && nrhs <= c->rmax) {
+        std::vector<int> sts(nrhs, ANL_OK);
+        ANL_TRY(pcg_batch<float>(c, nrhs, f, x, rtol, maxiter, iters, relres, sts.data(), s));
+        for (int k = 0; k < nrhs; ++k)
+            if (sts[k] != ANL_OK && worst == ANL_OK) worst = sts[k];
+        c->last_status.assign(sts.begin(), sts.end());
+    } else {
+        c->last_status.assign(nrhs, ANL_OK);
+        for (int k = 0; k < nrhs; ++k) {
+            int st = c->fp64 ? pcg_one<double>(c, f + k * n, x + k * n, rtol, maxiter, iters + k, relres + k, s)
+                             : pcg_one<float>(c, f + k * n, x + k * n, rtol, maxiter, iters + k, relres + k, s);
+            if (st == ANL_ERR_CUDA) return st;
+            c->last_status[k] = st;
+            if (st != ANL_OK && worst == ANL_OK) worst = st;
+        }
     }
     if (worst == ANL_ERR_MAXITER) set_error("CG did not reach rtol %.3g in %d iterations", rtol, maxiter);
     if (worst == ANL_ERR_NONFINITE) set_error("a non-finite value appeared in CG");

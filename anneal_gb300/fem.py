@@ -144,11 +144,14 @@ class StiffnessOperator:
 class FEM:
     """Linear elastic solve on the active voxels of a grid (fem.py:130-263)."""
 
-    def __init__(self, grid, active, fixed_dofs, nu, log=None, precision="auto"):
+    def __init__(self, grid, active, fixed_dofs, nu, log=None, precision="auto", multi="batch"):
         require_cuda()
         if precision not in ("auto", "fp32", "fp64"):
             raise ValueError(f"precision must be 'auto', 'fp32' or 'fp64', not {precision!r}")
+        if multi not in ("batch", "lanes"):
+            raise ValueError(f"multi must be 'batch' or 'lanes', not {multi!r}")
         self.precision = precision
+        self.multi = multi
         t0 = time.time()
         self.grid = grid
         self.nu = float(nu)
@@ -176,12 +179,13 @@ class FEM:
         self.log(f"  system: {self.act.size:,} elements, {self.nfree:,} free dofs, "
                  f"matrix-free on the GPU, built in {time.time() - t0:.1f} s")
 
-    def _ctx(self, fp64, lane=0):
+    def _ctx(self, fp64, lane=0, nrhs=1):
         """The solver context of a precision; lanes > 0 are extra contexts that solve other
-        load cases at the same time, each on its own stream."""
-        key = ("fp64" if fp64 else "fp32", lane)
+        load cases at the same time, each on its own stream; nrhs > 1 is an FP32 context
+        that solves that many cases together."""
+        key = ("fp64" if fp64 else "fp32", lane, nrhs)
         if key not in self._ctxs:
-            c = Context(self.grid.shape, self.grid.h, self.nu, fp64=fp64)
+            c = Context(self.grid.shape, self.grid.h, self.nu, fp64=fp64, nrhs=nrhs)
             c.set_domain(self.active_t, self.fixed_t)
             self._ctxs[key] = c
         return self._ctxs[key]
@@ -210,9 +214,11 @@ class FEM:
         The reference solves its load cases one after the other (fem.py:217-231). Here the
         cases are solved as a batch: a case whose load is a scalar multiple of another's
         (for example the +x / -x pair of a load set) takes that multiple of its solution,
-        because the problem is linear; the remaining distinct cases run at the same time,
-        each in its own context and stream, so the latency-bound coarse levels of their
-        V-cycles overlap on the GPU."""
+        because the problem is linear; the remaining distinct cases run at the same time.
+        With ``multi="batch"`` (the default) an FP32 solve advances all of them in the same
+        kernels (one context with a slot per case: the latency-bound coarse levels of the
+        V-cycle get that many times the work per launch); with ``multi="lanes"``, and for
+        FP64 solves, each case runs in its own context and stream."""
         fp64 = self.fp64_for(rtol)
         nrhs = F.shape[0] if F.dim() == 2 else 1
         if nrhs == 1:
@@ -224,7 +230,10 @@ class FEM:
         else:
             groups = self._multiple_groups(F, fp64)
             reps = [g[0] for g in groups]
-            res = self._solve_lanes(escale, F, X, reps, rtol, maxiter, rebuild, fp64)
+            if not fp64 and self.multi == "batch" and len(reps) > 1:
+                res = self._solve_batch(escale, F, X, reps, rtol, maxiter, rebuild)
+            else:
+                res = self._solve_lanes(escale, F, X, reps, rtol, maxiter, rebuild, fp64)
             iters, relres, sts = [0] * nrhs, [0.0] * nrhs, []
             for (rep, members), (st, it, rr) in zip(groups, res):
                 sts.append(st)
@@ -271,6 +280,27 @@ class FEM:
             if not placed:
                 groups.append((i, []))
         return groups
+
+    def _solve_batch(self, escale, F, X, reps, rtol, maxiter, rebuild):
+        """Solves F[reps] together in one FP32 context with len(reps) slots; a case that
+        stagnates above rtol in FP32 is finished in FP64 from its FP32 iterate. Returns
+        [(status, iters, relres)]."""
+        R = len(reps)
+        idx = torch.as_tensor(reps, device=F.device)
+        Fb = F.index_select(0, idx).contiguous()
+        Xb = X.index_select(0, idx).contiguous()
+        ctx = self._ctx(False, nrhs=R)
+        st, its, rrs = ctx.solve(escale, Fb, Xb, rtol, maxiter, rebuild)
+        out = []
+        for k in range(R):
+            sk = ctx.solve_status(k) if st != N.ANL_OK else N.ANL_OK
+            it, rr = its[k], rrs[k]
+            if sk == N.ANL_ERR_STAGNATION:  # finish in FP64 from the FP32 iterate
+                sk, it2, r2 = self._ctx(True).solve(escale, Fb[k:k + 1], Xb[k:k + 1], rtol, maxiter, rebuild)
+                it, rr = it + it2[0], r2[0]
+            out.append((sk, it, rr))
+        X.index_copy_(0, idx, Xb)
+        return out
 
     def _solve_lanes(self, escale, F, X, reps, rtol, maxiter, rebuild, fp64):
         """Solves F[reps[k]] in context lane k on stream k, concurrently (host threads; the

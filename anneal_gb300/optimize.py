@@ -67,13 +67,13 @@ class SimpRunner:
 
     def __init__(self, grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=80, r_mm=None,
                  p_final=3.0, move=0.2, combine="sum", log=print, x0=None, beta_max=BETA_MAX, rtol=None,
-                 maxiter=2000, warm_start=None, precision="auto"):
+                 maxiter=2000, warm_start=None, precision="auto", multi="batch"):
         self.grid = grid
         self.E0, self.vf, self.iters, self.p_final, self.move = float(E0), float(vf), int(iters), p_final, move
         self.combine, self.log, self.beta_max, self.maxiter = combine, log, beta_max, maxiter
         self.emin = EMIN
         self.rtol = CG_RTOL if rtol is None else float(rtol)
-        self.fem = fem = FEM(grid, active, fixed, nu, log=log, precision=precision)
+        self.fem = fem = FEM(grid, active, fixed, nu, log=log, precision=precision, multi=multi)
         self.ctx = ctx = fem._ctx(fp64=False)
         act = self.act = fem.act
         ne = grid.nelem
@@ -269,14 +269,15 @@ class SimpRunner:
 
 def simp(grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf,
          iters=80, r_mm=None, p_final=3.0, move=0.2, combine="sum", log=print, tol=0.01, x0=None,
-         beta_max=BETA_MAX, rtol=None, maxiter=2000, precision="auto"):
+         beta_max=BETA_MAX, rtol=None, maxiter=2000, precision="auto", multi="batch"):
     """optimize.py:50-180 on the GPU. ``rtol`` overrides the CG tolerance (default CG_RTOL,
     the reference's hard-coded 1e-6); the void stiffness is the module constant EMIN.
-    ``precision`` ("auto", "fp32", "fp64") picks the solver's operator arithmetic (FEM)."""
+    ``precision`` ("auto", "fp32", "fp64") picks the solver's operator arithmetic and
+    ``multi`` ("batch", "lanes") how several load cases are solved (FEM)."""
     t_start = time.time()
     run = SimpRunner(grid, fill, active, frozen, fixed, loads, weights, E0, nu, vf, iters=iters, r_mm=r_mm,
                      p_final=p_final, move=move, combine=combine, log=log, x0=x0, beta_max=beta_max, rtol=rtol,
-                     maxiter=maxiter, precision=precision)
+                     maxiter=maxiter, precision=precision, multi=multi)
     for _ in range(iters):
         run.step()
         if run.converged(tol):

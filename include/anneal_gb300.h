@@ -37,6 +37,10 @@ enum {
 };
 
 enum { ANL_FLAG_FP64 = 1 /* K u, smoothers and CG vectors in FP64 (default: FP32) */ };
+/* Right-hand-side slots of an FP32 context (flags bits 8-15, 1..255; default 1): anl_solve
+   with 1 < nrhs <= n solves its cases together, see anl_solve. Each slot holds its own CG
+   vectors and V-cycle vectors on every level (about 60 bytes per node). */
+#define ANL_FLAG_RHS(n) ((int)(n) << 8)
 
 int anl_version(void);
 /* Text of the last error in the calling thread ("" if none). */
@@ -65,8 +69,11 @@ int anl_free_mask(anl_ctx* ctx, uint8_t* mask, anl_stream_t stream);
    float (default context) or double (ANL_FLAG_FP64). */
 int anl_apply_K(anl_ctx* ctx, const float* escale, const void* u, void* y, anl_stream_t stream);
 
-/* Replaces FEM.solve (fem.py:206-232): solves K x = f for nrhs right-hand sides, one after
-   another, by CG preconditioned with a geometric-multigrid V-cycle. f and x are nrhs
+/* Replaces FEM.solve (fem.py:206-232): solves K x = f for nrhs right-hand sides by CG
+   preconditioned with a geometric-multigrid V-cycle: one after another, as the reference does,
+   or, in an FP32 context created with ANL_FLAG_RHS(R) and 1 < nrhs <= R, together (every kernel
+   of an iteration advances all cases, each with its own CG scalars, residual replacements and
+   acceptance; a case's iterates are those of its own solve). f and x are nrhs
    consecutive nodal vectors (double); x holds the initial guesses on entry (x0_list).
    rebuild != 0 re-estimates the smoother spectra and refactors the coarse grid (the
    reference's AMG rebuild, fem.py:207-216); otherwise the last ones are kept. iters / relres
@@ -82,6 +89,11 @@ int anl_apply_K(anl_ctx* ctx, const float* escale, const void* u, void* y, anl_s
    SolverError. */
 int anl_solve(anl_ctx* ctx, const float* escale, const double* f, double* x, int nrhs, double rtol,
               int maxiter, int rebuild, int* iters, double* relres, anl_stream_t stream);
+
+/* Status of right-hand side k (0 <= k < nrhs) in the last anl_solve on this context (ANL_OK,
+   ANL_ERR_MAXITER, ...); anl_solve itself returns the first non-OK one. No reference
+   counterpart: the reference raises on the first failing case (fem.py:225-229). */
+int anl_solve_status(const anl_ctx* ctx, int k);
 
 /* sum over DOFs of a[i] * b[i] (double vectors): the compliance f @ u (optimize.py:125). */
 int anl_dot(anl_ctx* ctx, const double* a, const double* b, double* out_h, anl_stream_t stream);

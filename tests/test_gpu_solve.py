@@ -229,14 +229,53 @@ def test_six_load_cases_batched_match_one_by_one():
     fem.close()
 
 
-def test_six_case_simp_matches_oracle(oracle):
+def test_fp32_batch_is_the_one_by_one_solve():
+    """FP32 cases solved together in one context (a slot per case, every kernel advancing all
+    of them) take exactly the iterates of their own solves: bit-identical solutions and the
+    same CG iterations as one solve per case and as concurrent lanes. A zero load among them
+    returns a zero solution in 0 iterations."""
+    import torch
+    w = P.six_case_bracket(scale=1.0 / 6.0)
+    grid = _grid(w.shape)
+    rng = np.random.default_rng(11)
+    E = np.exp(rng.normal(0.0, 1.0, w.nelem)) * w.active
+    escale = torch.as_tensor(E, dtype=torch.float32, device="cuda")
+    res = {}
+    for multi in ("batch", "lanes"):
+        fem = G.FEM(grid, w.active, w.fixed, 0.3, precision="fp32", multi=multi)
+        mask = fem._mask_t.double()
+        F = torch.stack([torch.as_tensor(w.loads[k], device="cuda") * mask for k in w.loads] +
+                        [torch.zeros_like(mask)])
+        X = torch.zeros_like(F)
+        its = fem.solve_device(escale, F, X, rtol=1e-6)
+        res[multi] = (X, its, fem)
+    Xb, itb, fem = res["batch"]
+    Xl, itl, _ = res["lanes"]
+    assert any(k[2] > 1 for k in fem._ctxs)  # the batched context was used
+    assert itb == itl and torch.equal(Xb, Xl)
+    assert itb[-1] == 0 and float(Xb[-1].abs().max()) == 0.0
+    for i in range(Xb.shape[0] - 1):
+        Xi = torch.zeros_like(Xb[i:i + 1])
+        it = fem.solve_device(escale, (torch.as_tensor(w.loads[list(w.loads)[i]], device="cuda") *
+                                       fem._mask_t.double())[None], Xi, rtol=1e-6)
+        assert it[0] == itb[i] and torch.equal(Xi[0], Xb[i]), i
+    for _, _, f in res.values():
+        f.close()
+
+
+@pytest.mark.parametrize("precision,rtol", [("auto", 1e-8), ("fp32", 1e-6)])
+def test_six_case_simp_matches_oracle(oracle, precision, rtol):
+    """Six load cases (+-x, +-y, +-z: each negative case folded onto its positive one, the
+    three distinct cases solved together) through four SIMP iterations: FP64 lanes at rtol
+    1e-8 and the FP32 batch at rtol 1e-6."""
     w = P.six_case_bracket(scale=1.0 / 6.0)
     kw = dict(iters=4, r_mm=1.5, p_final=3.0, move=0.2, tol=0.0, x0=np.full(w.nelem, 0.25), beta_max=0.0,
-              log=lambda *a: None, rtol=1e-8)
+              log=lambda *a: None, rtol=rtol)
     old = O.EMIN
     O.EMIN = 1e-9
     try:
-        got = O.simp(_grid(w.shape), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, 1.0, 0.3, 0.25, **kw)
+        got = O.simp(_grid(w.shape), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, 1.0, 0.3, 0.25,
+                     precision=precision, **kw)
     finally:
         O.EMIN = old
     want = oracle.simp(w.shape, 1.0, w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, 1.0, 0.3, 0.25,
