@@ -158,7 +158,7 @@ def _lbracket_run(golden, name, scale):
         hist = [run.step() for _ in range(int(s["iters"]))]
         x = np.zeros(w.nelem)
         x[run.act] = run.xphys_t.cpu().numpy().astype(float)[run.act]
-        assert not run.fem._ctxs.get(("fp64", 0)), "an FP32 solve fell back to FP64"
+        assert not run.fem._ctxs.get(("fp64", 0, 1)), "an FP32 solve fell back to FP64"
         run.close()
         torch.cuda.empty_cache()
     finally:
@@ -261,6 +261,40 @@ def test_fp32_batch_is_the_one_by_one_solve():
         assert it[0] == itb[i] and torch.equal(Xi[0], Xb[i]), i
     for _, _, f in res.values():
         f.close()
+
+
+def test_six_case_bracket_160_fp32_batch_matches_oracle(golden):
+    """The six-case bracket at full size (160x80x80, 3.17M DOF per case) through the FP32
+    batch (the three distinct cases in one context), its first 3 SIMP iterations against the
+    oracle, which solves all six cases one after another: every case's compliance within
+    1e-5, the density within 1e-3."""
+    import torch
+    s = golden("sixcase160_3it.npz")
+    w = P.six_case_bracket(scale=5.0 / 6.0, vf=0.25, r_vox=2.0, emin=1e-9)
+    assert tuple(s["shape"]) == w.shape
+    old = O.EMIN
+    O.EMIN = 1e-9
+    try:
+        run = O.SimpRunner(_grid(w.shape), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, w.E0, w.nu,
+                           w.vf, iters=int(s["iters"]), r_mm=w.r_vox, p_final=3.0, move=0.2,
+                           x0=np.full(w.nelem, w.vf), beta_max=0.0, rtol=float(s["rtol"]), log=lambda *a: None,
+                           precision="fp32", multi="batch")
+        hist = [run.step() for _ in range(int(s["iters"]))]
+        x = np.zeros(w.nelem)
+        x[run.act] = run.xphys_t.cpu().numpy().astype(float)[run.act]
+        assert ("fp32", 0, 3) in run.fem._ctxs, "the three distinct cases were not batched"
+        assert not run.fem._ctxs.get(("fp64", 0, 1)), "an FP32 solve fell back to FP64"
+        run.close()
+        torch.cuda.empty_cache()
+    finally:
+        O.EMIN = old
+    c = np.array([h["compliance"] for h in hist])
+    assert c.shape == s["h_compliance_cases"].shape
+    assert np.abs(c / s["h_compliance_cases"] - 1).max() < 1e-5
+    assert np.abs(np.array([h["volumeFraction"] for h in hist]) - s["h_volumeFraction"]).max() < 1e-5
+    assert np.abs(x[::17] - s["x_q16_stride17"] / 65535.0).max() < 1e-3
+    nx = int(s["shape"][0])
+    assert np.abs(x.reshape(-1, nx).sum(axis=1) - s["row_sums"]).max() < 1e-3 * nx
 
 
 @pytest.mark.parametrize("precision,rtol", [("auto", 1e-8), ("fp32", 1e-6)])
