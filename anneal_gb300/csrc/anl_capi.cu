@@ -425,11 +425,11 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     // the V-cycle tail: the first level (level 2 or below, on the box levels) from which every
     // level to the coarsest fits one CTA (at most 1024 elements, the vectors in shared memory)
     {
-        // opt-in (ANL_TAIL=1): on the 256x128x128 bench workload the one-CTA tail (levels 4-6)
-        // measured slower than the same levels as separate launches in the CUDA graph (33.2
-        // against 33.8 SIMP iterations/s, the same CG iterations)
+        // on by default (ANL_TAIL=0 turns it off): on the 256x128x128 L-bracket the tail takes
+        // levels 4-6 in 104 us per V-cycle against about 180 us for their 35 launches, 34.7
+        // against 33.9 SIMP iterations/s at the same CG iterations
         const char* e = std::getenv("ANL_TAIL");
-        const bool tail_on = e && std::atoi(e) != 0;
+        const bool tail_on = !(e && std::atoi(e) == 0);
         const int nl = (int)c->lev.size();
         if (tail_on && !c->fp64 && c->dense_coarse && nl >= 2) {
             for (int l = std::max(c->box_from, 2); l <= nl - 2 && c->tail_from < 0; ++l) {

@@ -163,6 +163,10 @@ struct TailArgs {
     int nc = 0;
     const int* done = nullptr;
     KeModal<float> km{};
+    // right-hand-side slots: CTA r works on slot r (b0, x0 and done offset by these strides)
+    int nrhs = 1;
+    int64_t vstride = 0;  // floats between the slots' vectors of the first tail level
+    int sc_bytes = 0;     // bytes between the slots' done flags
 };
 size_t tail_smem_bytes(const TailLevel* lev, int nlev);
 int vtail_prepare();

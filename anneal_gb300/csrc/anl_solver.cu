@@ -1160,7 +1160,8 @@ static int vcycle_box(anl_ctx* c, size_t l, int deg, const int* done, cudaStream
     return ANL_OK;
 }
 
-// The levels from tail_from down in one CTA: b of level l in, its correction x out.
+// The levels from tail_from down in one CTA per right-hand-side slot: b of level l in, its
+// correction x out.
 static int vcycle_tail(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     TailArgs a;
     a.nlev = (int)(c->lev.size() - l);
@@ -1180,13 +1181,16 @@ static int vcycle_tail(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     a.nc = c->nc;
     a.done = done;
     a.km = c->kmf;
+    a.nrhs = c->rb;
+    a.vstride = c->lev[l].vs;
+    a.sc_bytes = (int)sizeof(PcgScalars);
     return launch_vtail(a, s);
 }
 
 template <class T>
 static int vcycle(anl_ctx* c, size_t l, const int* done, cudaStream_t s) {
     Level& L = c->lev[l];
-    if (sizeof(T) == 4 && c->rb == 1 && c->tail_from >= 0 && (int)l == c->tail_from) return vcycle_tail(c, l, done, s);
+    if (sizeof(T) == 4 && c->tail_from >= 0 && (int)l == c->tail_from) return vcycle_tail(c, l, done, s);
     if (l + 1 == c->lev.size()) {
         if (c->dense_coarse) {
             const int n = c->nc;

@@ -357,7 +357,7 @@ def test_box_smoother_levels_match_the_marching_kernel(monkeypatch):
 
 
 def test_one_cta_vcycle_tail_matches_per_level_launches(monkeypatch):
-    """The smallest multigrid levels and the coarsest solve in one CTA (ANL_TAIL=1) against the
+    """The smallest multigrid levels and the coarsest solve in one CTA (the default) against the
     same levels as separate launches: the same solution to the tolerance and about the same CG
     iterations, on two grids (a cantilever and the L-bracket with its void)."""
     import torch
