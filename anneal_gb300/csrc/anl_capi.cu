@@ -237,6 +237,7 @@ static void free_ctx(anl_ctx* c) {
     f(c->A);
     f(c->Ainv);
     f(c->ainv_hi);
+    f(c->sens_df);
     f(c->ainv_lo);
     f(c->flag_d);
     f(c->restart_d);
@@ -396,8 +397,8 @@ static int create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, in
     ALLOC(c->sc, R * sizeof(PcgScalars));
     c->part_cap = std::max(ku_grid_blocks(c->d), kRedBlocks);
     {
-        // the filter reduction grid (32x4x2 tiles) can exceed both
-        const int fb = ceil_div(c->d.nx, 32) * ceil_div(c->d.ny, 4) * ceil_div(c->d.nz, 2);
+        // the filter reduction grid (32 x 8 columns of 16 layers) can exceed both
+        const int fb = ceil_div(c->d.nx, 32) * ceil_div(c->d.ny, 8) * ceil_div(c->d.nz, 16);
         c->part_cap = std::max(c->part_cap, fb);
     }
     c->part_stride = (int64_t)c->part_cap * kMaxRedVals;

@@ -446,6 +446,13 @@ __device__ __forceinline__ DF operator*(DF a, DF b) {
     return df_norm(p, e);
 }
 __device__ __forceinline__ DF operator/(DF a, DF b) { return DF(a.value() / b.value()); }  // not on a hot path
+// 1 / a to about 48 bits: the FP32 reciprocal refined by one Newton step in pair arithmetic
+// (r + r (1 - a r) doubles the number of correct bits)
+__device__ __forceinline__ DF df_recip(DF a) {
+    const float r0 = 1.f / a.hi;
+    const DF e = DF(1.f) - a * DF(r0);
+    return DF(r0) + DF(r0) * e;
+}
 __device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
 __device__ __forceinline__ bool operator>(DF a, DF b) { return a.value() > b.value(); }
 #endif

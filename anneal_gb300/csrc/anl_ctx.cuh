@@ -101,6 +101,8 @@ struct anl_ctx {
     double* bbuf_base = nullptr;
     void* bdf_base = nullptr;
     anl::PcgScalars* sc_base = nullptr;
+    anl::DF* sens_df = nullptr;  // the sensitivity's displacements as float pairs (grows)
+    size_t sens_df_cap = 0;
     float* ainv_hi = nullptr;  // the coarsest dense inverse as float pairs (the tail's coarse solve)
     float* ainv_lo = nullptr;
 #ifndef ANL_CHEB_LO

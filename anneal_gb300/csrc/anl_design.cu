@@ -16,11 +16,14 @@ static inline int dgrid(int64_t n) { return (int)std::max<int64_t>(1, std::min<i
 
 // ------------------------------------------------------------------ density filter
 
-// Filter (optimize.py:24-47). One CTA of 32x4x2 threads owns a 32x4x2 tile of elements
-// and stages the tile plus an R-element halo in shared memory.
+// Filter (optimize.py:24-47). One CTA of 32x8 threads owns a 32x8 column of elements over
+// FT_ZC layers and marches up z: a ring of 2R + 2 element planes (each with an R-element halo
+// in x and y) in shared memory, one new plane staged per layer, one barrier per layer (the ring
+// has one slot more than the stencil reads, so the next plane never lands in a slot in use).
+// The taps are summed in (dz, dy, dx) order.
 enum { F_HS = 0, F_FWD = 1, F_BWD = 2, F_PHYS = 3, F_OCVOL = 4 };
 
-constexpr int FT_X = 32, FT_Y = 4, FT_Z = 2, FT_N = FT_X * FT_Y * FT_Z;
+constexpr int FT_X = 32, FT_Y = 8, FT_ZC = 16, FT_N = FT_X * FT_Y;
 
 struct FilterArgs {
     Dims d;
@@ -74,70 +77,128 @@ __device__ __forceinline__ float oc_xn(float x, float dcx, float dvx, float lam,
     return oc_xn(oc_elem(x, dcx, dvx, move), lam, oc_rl(lam));
 }
 
+// the filter's input value of element (gi, gj, gk) (zero outside the grid and on inactive
+// elements): the active flag and the field are loaded independently of each other
 template <int MODE>
+__device__ __forceinline__ float filter_input(const FilterArgs& a, int gi, int gj, int gk) {
+    const Dims& d = a.d;
+    if (gi < 0 || gj < 0 || gk < 0 || gi >= d.nx || gj >= d.ny || gk >= d.nz) return 0.f;
+    const int64_t e = d.elem(gi, gj, gk);
+    const bool act = a.active[e] != 0;
+    float v = 1.f;
+    if (MODE == F_FWD || MODE == F_PHYS) v = a.in[e];
+    else if (MODE == F_BWD) v = a.in[e] / a.Hs[e];
+    else if (MODE == F_OCVOL) v = a.frozen[e] ? 1.f : oc_xn(a.x[e], a.dcx[e], a.dvx[e], a.lam, a.move);
+    return act ? v : 0.f;
+}
+
+// RT: the halo at compile time (1: the 27-tap cone of radii up to 2, weights in registers),
+// or 0 for any R up to kMaxFilterR
+template <int MODE, int RT>
 __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
     extern __shared__ float sm[];
     const Dims d = a.d;
-    const int R = a.R, W = 2 * R + 1;
-    const int TX = FT_X + 2 * R, TY = FT_Y + 2 * R, TZ = FT_Z + 2 * R;
-    float* tile = sm;
-    float* wts = sm + TX * TY * TZ;
-    const int tid = threadIdx.x + FT_X * (threadIdx.y + FT_Y * threadIdx.z);
-    const int i0 = blockIdx.x * FT_X, j0 = blockIdx.y * FT_Y, k0 = blockIdx.z * FT_Z;
+    const int R = RT > 0 ? RT : a.R, W = 2 * R + 1;
+    const int TX = FT_X + 2 * R, TY = FT_Y + 2 * R, PL = TX * TY, NS = W + 1;  // ring of NS planes
+    float* ring = sm;
+    float* wts = sm + NS * PL;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + FT_X * ty;
+    const int i0 = blockIdx.x * FT_X, j0 = blockIdx.y * FT_Y, kb = blockIdx.z * FT_ZC;
+    const int kend = min(kb + FT_ZC, d.nz);
     for (int t = tid; t < W * W * W; t += FT_N) wts[t] = a.w[t];
-    for (int t = tid; t < TX * TY * TZ; t += FT_N) {
-        const int tx = t % TX, ty = (t / TX) % TY, tz = t / (TX * TY);
-        const int gi = i0 - R + tx, gj = j0 - R + ty, gk = k0 - R + tz;
-        float v = 0.f;
-        if (gi >= 0 && gj >= 0 && gk >= 0 && gi < d.nx && gj < d.ny && gk < d.nz) {
-            const int64_t e = d.elem(gi, gj, gk);
-            if (a.active[e]) {
-                if (MODE == F_HS) v = 1.f;
-                else if (MODE == F_FWD || MODE == F_PHYS) v = a.in[e];
-                else if (MODE == F_BWD) v = a.in[e] / a.Hs[e];
-                else if (MODE == F_OCVOL) v = a.frozen[e] ? 1.f : oc_xn(a.x[e], a.dcx[e], a.dvx[e], a.lam, a.move);
-            }
+    // stage element plane gk into its ring slot
+    auto stage = [&](int gk) {
+        float* pl = ring + ((gk + NS * (kMaxFilterR + 1)) % NS) * PL;
+        for (int y = ty; y < TY; y += FT_Y)
+            for (int x = tx; x < TX; x += FT_X) pl[y * TX + x] = filter_input<MODE>(a, i0 - R + x, j0 - R + y, gk);
+    };
+    // the next plane's values of this thread, loaded a layer ahead (registers; the plane of a
+    // 27-tap filter is 34 x 10 values, at most 2 per thread)
+    constexpr int PF = RT == 1 ? (34 * 10 + FT_N - 1) / FT_N : 1;
+    float pf[PF];
+    auto prefetch = [&](int gk) {
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            const int t = tid + q * FT_N, y = t / (FT_X + 2), x = t - y * (FT_X + 2);
+            pf[q] = t < PL ? filter_input<MODE>(a, i0 - 1 + x, j0 - 1 + y, gk) : 0.f;
         }
-        tile[t] = v;
-    }
+    };
+    auto commit = [&](int gk) {
+        float* pl = ring + ((gk + NS * (kMaxFilterR + 1)) % NS) * PL;
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            const int t = tid + q * FT_N;
+            if (t < PL) pl[t] = pf[q];
+        }
+    };
+    for (int gk = kb - R; gk < kb + R; ++gk) stage(gk);
+    if (RT == 1) prefetch(kb + R);
     __syncthreads();
-    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y, k = k0 + threadIdx.z;
+    float wr[RT > 0 ? 27 : 1];
+    if (RT == 1) {
+#pragma unroll
+        for (int q = 0; q < (RT > 0 ? 27 : 1); ++q) wr[q] = wts[q];
+    }
+    const int i = i0 + tx, j = j0 + ty;
+    const bool in_xy = i < d.nx && j < d.ny;
     double vol = 0.0;
-    if (i < d.nx && j < d.ny && k < d.nz) {
-        float s = 0.f;
-        for (int dz = 0; dz < W; ++dz)
-            for (int dy = 0; dy < W; ++dy) {
-                const float* row = tile + ((threadIdx.z + dz) * TY + (threadIdx.y + dy)) * TX + threadIdx.x;
-                const float* wr = wts + (dz * W + dy) * W;
-                for (int dx = 0; dx < W; ++dx) s = fmaf(wr[dx], row[dx], s);
-            }
-        const int64_t e = d.elem(i, j, k);
-        const bool act = a.active[e] != 0;
-        if (MODE == F_HS) {
-            a.out[e] = s == 0.f ? 1.f : s;
-        } else if (MODE == F_FWD) {
-            a.out[e] = act ? s / a.Hs[e] : 0.f;
-        } else if (MODE == F_BWD) {
-            a.out[e] = act ? s : 0.f;
+    for (int k = kb; k < kend; ++k) {
+        if (RT == 1) {  // plane k + 1 was loaded during the previous layer; load plane k + 2
+            commit(k + 1);
+            if (k + 1 < kend) prefetch(k + 2);
         } else {
-            // physical(): projection (optimize.py:81-87), frozen -> 1 (optimize.py:92)
-            float xt = act ? s / a.Hs[e] : 0.f;
-            float xp = xt, g = 1.f;
-            if (a.beta > 0.f) {
-                const float th = tanhf(a.beta * (xt - a.eta));
-                xp = (a.t0 + th) / (a.t0 + a.t1);
-                g = a.beta * (1.f - th * th) / (a.t0 + a.t1);
-            }
-            if (a.frozen[e]) xp = 1.f;
-            if (!act) {
-                xp = 0.f;
-                g = 0.f;
-            }
-            if (MODE == F_PHYS) {
-                a.out[e] = xp;
-                if (a.dxp) a.dxp[e] = g;
+            stage(k + R);
+        }
+        __syncthreads();
+        if (in_xy) {
+            float s = 0.f;
+            if (RT == 1) {
+#pragma unroll
+                for (int dz = 0; dz < 3; ++dz) {
+                    const float* pl = ring + ((k - 1 + dz + NS * (kMaxFilterR + 1)) % NS) * PL;
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                        for (int dx = 0; dx < 3; ++dx) s = fmaf(wr[(dz * 3 + dy) * 3 + dx], pl[(ty + dy) * TX + tx + dx], s);
+                }
             } else {
-                vol = act ? (double)a.phi[e] * (double)xp : 0.0;
+                for (int dz = 0; dz < W; ++dz) {
+                    const float* pl = ring + ((k - R + dz + NS * (kMaxFilterR + 1)) % NS) * PL;
+                    for (int dy = 0; dy < W; ++dy) {
+                        const float* row = pl + (ty + dy) * TX + tx;
+                        const float* w = wts + (dz * W + dy) * W;
+                        for (int dx = 0; dx < W; ++dx) s = fmaf(w[dx], row[dx], s);
+                    }
+                }
+            }
+            const int64_t e = d.elem(i, j, k);
+            const bool act = a.active[e] != 0;
+            if (MODE == F_HS) {
+                a.out[e] = s == 0.f ? 1.f : s;
+            } else if (MODE == F_FWD) {
+                a.out[e] = act ? s / a.Hs[e] : 0.f;
+            } else if (MODE == F_BWD) {
+                a.out[e] = act ? s : 0.f;
+            } else {
+                // physical(): projection (optimize.py:81-87), frozen -> 1 (optimize.py:92)
+                float xt = act ? s / a.Hs[e] : 0.f;
+                float xp = xt, g = 1.f;
+                if (a.beta > 0.f) {
+                    const float th = tanhf(a.beta * (xt - a.eta));
+                    xp = (a.t0 + th) / (a.t0 + a.t1);
+                    g = a.beta * (1.f - th * th) / (a.t0 + a.t1);
+                }
+                if (a.frozen[e]) xp = 1.f;
+                if (!act) {
+                    xp = 0.f;
+                    g = 0.f;
+                }
+                if (MODE == F_PHYS) {
+                    a.out[e] = xp;
+                    if (a.dxp) a.dxp[e] = g;
+                } else {
+                    vol += act ? (double)a.phi[e] * (double)xp : 0.0;
+                }
             }
         }
     }
@@ -158,20 +219,23 @@ static int launch_filter(anl_ctx* c, int mode, FilterArgs a, cudaStream_t s) {
     a.active = c->active;
     a.Hs = c->filt.Hs;
     const int W = 2 * a.R + 1;
-    const size_t smem = sizeof(float) * ((FT_X + 2 * a.R) * (FT_Y + 2 * a.R) * (FT_Z + 2 * a.R) + W * W * W);
-    dim3 grid(ceil_div(d.nx, FT_X), ceil_div(d.ny, FT_Y), ceil_div(d.nz, FT_Z)), block(FT_X, FT_Y, FT_Z);
+    const size_t smem = sizeof(float) * ((W + 1) * (FT_X + 2 * a.R) * (FT_Y + 2 * a.R) + W * W * W);
+    dim3 grid(ceil_div(d.nx, FT_X), ceil_div(d.ny, FT_Y), ceil_div(d.nz, FT_ZC)), block(FT_X, FT_Y);
     if (mode == F_OCVOL && (int64_t)grid.x * grid.y * grid.z > c->part_cap) {
         set_error("filter reduction needs %d blocks, scratch holds %d", grid.x * grid.y * grid.z, c->part_cap);
         return ANL_ERR_BADARG;
     }
+#define F_LAUNCH(M)                                                              \
+    (a.R == 1 ? k_filter<M, 1><<<grid, block, smem, s>>>(a) : k_filter<M, 0><<<grid, block, smem, s>>>(a))
     switch (mode) {
-        case F_HS: k_filter<F_HS><<<grid, block, smem, s>>>(a); break;
-        case F_FWD: k_filter<F_FWD><<<grid, block, smem, s>>>(a); break;
-        case F_BWD: k_filter<F_BWD><<<grid, block, smem, s>>>(a); break;
-        case F_PHYS: k_filter<F_PHYS><<<grid, block, smem, s>>>(a); break;
-        case F_OCVOL: k_filter<F_OCVOL><<<grid, block, smem, s>>>(a); break;
+        case F_HS: F_LAUNCH(F_HS); break;
+        case F_FWD: F_LAUNCH(F_FWD); break;
+        case F_BWD: F_LAUNCH(F_BWD); break;
+        case F_PHYS: F_LAUNCH(F_PHYS); break;
+        case F_OCVOL: F_LAUNCH(F_OCVOL); break;
         default: return ANL_ERR_BADARG;
     }
+#undef F_LAUNCH
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }
@@ -258,7 +322,7 @@ constexpr int kMaxCases = 16;
 struct SensArgs {
     Dims d;
     const uint8_t* active;
-    const double* u;  // nrhs nodal vectors
+    const DF* u;      // nrhs nodal vectors as float pairs (k_split_pairs)
     int nrhs;
     int64_t stride;   // 3 * nn
     float coef[kMaxCases];
@@ -271,22 +335,36 @@ struct SensArgs {
     int energy_only;
 };
 
+// The FP64 displacements as float pairs, once per node (split_double: no FP64 arithmetic);
+// the element kernel then reads each corner as one 8-byte pair instead of splitting it again
+// for each of its up to 8 elements.
+__global__ void k_split_pairs(int64_t n, const double* x, DF* xdf) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float h, l;
+        split_double(x[i], h, l);
+        xdf[i] = DF(h, l);
+    }
+}
+
 // u_e^T Ke u_e from the modal energy form (modal_energy): edge differences are formed in
-// FP64 and rounded to FP32, and rigid rotations cancel inside squares, so the result keeps its
-// accuracy relative to the element's own strain energy.
-__device__ __forceinline__ float element_energy(const KeModal<float>& K, const double* u, const Dims& d, int i, int j,
+// double-float arithmetic from the FP64 displacements and rounded once to FP32, and rigid
+// rotations cancel inside squares, so the result keeps its accuracy relative to the element's
+// own strain energy.
+__device__ __forceinline__ float element_energy(const KeModal<float>& K, const DF* u, const Dims& d, int i, int j,
                                                 int k) {
     const int64_t sx = 1, sy = d.nx + 1, sz = (int64_t)(d.nx + 1) * (d.ny + 1);
     const int64_t n0 = d.node(i, j, k);
-    // corner values as float pairs (split_double: no FP64 arithmetic), differences in
-    // double-float arithmetic rounded once to FP32
     float ch[2][2][2][3], cl[2][2][2][3];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int px = q & 1, py = (q >> 1) & 1, pz = (q >> 2) & 1;
         const int64_t n = n0 + px * sx + py * sy + pz * sz;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) split_double(__ldg(u + 3 * n + c), ch[px][py][pz][c], cl[px][py][pz][c]);
+        for (int c = 0; c < 3; ++c) {
+            const float2 t = __ldg(reinterpret_cast<const float2*>(u + 3 * n + c));
+            ch[px][py][pz][c] = t.x;
+            cl[px][py][pz][c] = t.y;
+        }
     }
     auto diff = [&](int ax, int bx, int ay, int by, int az, int bz) {
         V3<float> v;
@@ -394,12 +472,16 @@ int sensitivity(anl_ctx* c, const double* u, int nrhs, const double* coef, const
         set_error("sensitivity supports 1..%d load cases, got %d", kMaxCases, nrhs);
         return ANL_ERR_BADARG;
     }
+    const int64_t ndof = 3 * c->d.nn();
+    ANL_TRY(grow(c->sens_df, c->sens_df_cap, (size_t)nrhs * ndof, sizeof(DF)));
+    k_split_pairs<<<dgrid(nrhs * ndof), DT, 0, s>>>(nrhs * ndof, u, c->sens_df);
+    ANL_LAUNCH_CHECK();
     SensArgs a{};
     a.d = c->d;
     a.active = c->active;
-    a.u = u;
+    a.u = c->sens_df;
     a.nrhs = nrhs;
-    a.stride = 3 * c->d.nn();
+    a.stride = ndof;
     for (int k = 0; k < nrhs; ++k) a.coef[k] = coef ? (float)coef[k] : 1.f;
     a.xphys = xphys;
     a.dxp = dxp;

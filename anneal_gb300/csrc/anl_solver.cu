@@ -499,81 +499,89 @@ __global__ void __launch_bounds__(256) k_chol_inverse_smem(const double* L, doub
     for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i];
 }
 
-// The same factorisation and inverse in double-float arithmetic (about 48 bits, on the FP32
-// pipes: FP64 arithmetic on this part runs at a small fraction of FP32, and the factor's
-// trailing updates are ~n^3/6 multiply-adds on one SM). The matrix comes in as FP64 and is
-// split into float pairs without FP64 arithmetic (split_double); pivots, their square roots and
-// reciprocals (n of each) are taken in FP64. Tiny pivots are regularised as in k_cholesky.
-__device__ __forceinline__ DF df_fms(DF c, DF a, DF b) { return c - a * b; }  // c - a b
-
-__global__ void __launch_bounds__(1024) k_cholesky_df(double* A, int n, int* flag) {
-    extern __shared__ DF SD[];
-    __shared__ double piv, dmax;
+// The FP32 solver's coarsest grid in double-float arithmetic (about 48 bits, on the FP32 pipes:
+// FP64 arithmetic on this part runs at a small fraction of FP32, and the factor's trailing
+// updates are ~n^3/6 multiply-adds on one SM): A = L D L^T, no square roots. The matrix comes in
+// as FP64 and is split into float pairs without FP64 arithmetic (split_double). Each column
+// step is two phases with a barrier after each: the column of L (and an unscaled copy), then
+// the trailing update of the lower triangle, one warp per row. Every thread forms the pivot's
+// reciprocal itself, so the pivot needs no phase of its own. Tiny pivots are regularised as in
+// k_cholesky (to 1e-12 of the largest diagonal entry). On exit A holds L strictly below the
+// diagonal (unit diagonal implied) and D on it.
+__global__ void __launch_bounds__(1024) k_ldlt_df(double* A, int n, int* flag) {
+    extern __shared__ DF SD[];  // the matrix (n * n), then the unscaled column (n)
+    DF* ucol = SD + n * n;
+    __shared__ float dmax;
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
         float h, l;
         split_double(A[t], h, l);
         SD[t] = DF(h, l);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0.0;
-        for (int j = 0; j < n; ++j) m = fmax(m, SD[j * n + j].value());
-        dmax = m;
+    if (threadIdx.x < 32) {
+        float m = 0.f;
+        for (int j = threadIdx.x; j < n; j += 32) m = fmaxf(m, SD[j * n + j].hi);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) dmax = m;
     }
     __syncthreads();
+    const float floor_ = 1e-12f * dmax;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int j = 0; j < n; ++j) {
-        if (threadIdx.x == 0) {
-            const double a = SD[j * n + j].value();
-            if (!(a > 1e-12 * dmax)) {
+        DF a = SD[j * n + j];
+        if (!(a.hi > floor_)) {  // every thread takes the same branch (the value is idempotent)
+            a = DF(floor_);
+            if (threadIdx.x == 0) {
+                SD[j * n + j] = a;
                 *flag += 1;
-                piv = sqrt(1e-12 * dmax);
-            } else {
-                piv = sqrt(a);
             }
-            SD[j * n + j] = DF(piv);
+        }
+        const DF ia = df_recip(a);
+        for (int k = j + 1 + threadIdx.x; k < n; k += blockDim.x) {
+            const DF u = SD[k * n + j];
+            ucol[k] = u;
+            SD[k * n + j] = u * ia;
         }
         __syncthreads();
-        const DF rp = DF(1.0 / piv);
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) SD[i * n + j] = SD[i * n + j] * rp;
-        __syncthreads();
-        const int m = n - j - 1;
-        for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
-            const int i = j + 1 + t / m, k = j + 1 + t % m;
-            if (k <= i) SD[i * n + k] = df_fms(SD[i * n + k], SD[i * n + j], SD[k * n + j]);
+        for (int i = j + 1 + warp; i < n; i += nw) {
+            const DF lij = SD[i * n + j];
+            for (int k = j + 1 + lane; k <= i; k += 32) SD[i * n + k] = SD[i * n + k] - lij * ucol[k];
         }
         __syncthreads();
     }
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) A[t] = SD[t].value();
 }
 
-__global__ void __launch_bounds__(256) k_chol_inverse_df(const double* L, double* Ainv, int n) {
-    extern __shared__ DF SD[];  // L (n * n), reciprocal pivots (n), the column (n)
+// Column c of A^-1 from L D L^T (k_ldlt_df), one CTA per column: L y = e_c, z = D^-1 y,
+// L^T x = z, one barrier per step (each thread reads the settled entry of the step and
+// updates the others).
+__global__ void __launch_bounds__(256) k_ldlt_inverse_df(const double* LD, double* Ainv, int n) {
+    extern __shared__ DF SD[];  // L (n * n), 1 / D (n), the column (n)
     DF* rd = SD + n * n;
     DF* xs = rd + n;
     const int c = blockIdx.x;
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
         float h, l;
-        split_double(L[t], h, l);
+        split_double(LD[t], h, l);
         SD[t] = DF(h, l);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        rd[i] = DF(1.0 / L[i * n + i]);
+        rd[i] = df_recip(SD[i * n + i]);
         xs[i] = DF(i == c ? 1.f : 0.f);
     }
     __syncthreads();
-    for (int j = c; j < n; ++j) {  // L y = e_c (y_j = 0 for j < c)
-        const DF yj = xs[j] * rd[j];
-        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) xs[i] = df_fms(xs[i], SD[i * n + j], yj);
-        __syncthreads();
-        if (threadIdx.x == 0) xs[j] = yj;
+    for (int j = c; j < n - 1; ++j) {  // L y = e_c (y_j = 0 for j < c)
+        const DF yj = xs[j];
+        for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) xs[i] = xs[i] - SD[i * n + j] * yj;
         __syncthreads();
     }
-    for (int j = n - 1; j >= 0; --j) {  // L^T x = y
-        const DF xj = xs[j] * rd[j];
-        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] = df_fms(xs[i], SD[j * n + i], xj);
-        __syncthreads();
-        if (threadIdx.x == 0) xs[j] = xj;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = xs[i] * rd[i];
+    __syncthreads();
+    for (int j = n - 1; j > 0; --j) {  // L^T x = z
+        const DF xj = xs[j];
+        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] = xs[i] - SD[j * n + i] * xj;
         __syncthreads();
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) Ainv[(int64_t)i * n + c] = xs[i].value();
@@ -995,9 +1003,9 @@ static int coarse_factor(anl_ctx* c, cudaStream_t s) {
                                           kCholSmemN * kCholSmemN * (int)sizeof(double)));
             ANL_CUDA(cudaFuncSetAttribute(k_chol_inverse_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (kCholSmemN * kCholSmemN + 2 * kCholSmemN) * (int)sizeof(double)));
-            ANL_CUDA(cudaFuncSetAttribute(k_cholesky_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kCholSmemN * kCholSmemN * (int)sizeof(DF)));
-            ANL_CUDA(cudaFuncSetAttribute(k_chol_inverse_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            ANL_CUDA(cudaFuncSetAttribute(k_ldlt_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (kCholSmemN * kCholSmemN + kCholSmemN) * (int)sizeof(DF)));
+            ANL_CUDA(cudaFuncSetAttribute(k_ldlt_inverse_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (kCholSmemN * kCholSmemN + 2 * kCholSmemN) * (int)sizeof(DF)));
             attr = true;
         }
@@ -1007,9 +1015,9 @@ static int coarse_factor(anl_ctx* c, cudaStream_t s) {
             k_chol_inverse_smem<<<n, 256, ib, s>>>(c->A, c->Ainv, n);
             ANL_LAUNCH_CHECK();
         } else {  // the FP32 solver's preconditioner: double-float factor and inverse
-            k_cholesky_df<<<1, 1024, n * n * (int)sizeof(DF), s>>>(c->A, n, c->flag_d);
+            k_ldlt_df<<<1, 1024, (n * n + n) * (int)sizeof(DF), s>>>(c->A, n, c->flag_d);
             ANL_LAUNCH_CHECK();
-            k_chol_inverse_df<<<n, 256, (n * n + 2 * n) * (int)sizeof(DF), s>>>(c->A, c->Ainv, n);
+            k_ldlt_inverse_df<<<n, 256, (n * n + 2 * n) * (int)sizeof(DF), s>>>(c->A, c->Ainv, n);
             ANL_LAUNCH_CHECK();
         }
     } else {
