@@ -335,32 +335,102 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
 }
+// Block sum of NV float pairs (hi + lo per thread), entirely on the FP32 pipes: the warp tree
+// adds pairs with TwoSum, then thread 0 adds the warps' pairs in order. FP64 arithmetic on this
+// part runs at a small fraction of the FP32 rate: even a few FP64 instructions per warp, in every
+// block of a 1,216-block reduction, cost several microseconds. Result in thread 0 (in place).
 template <int NV, int NT>
-__device__ __forceinline__ void block_sum_f2(const float (&s)[NV], const float (&c)[NV], double (&val)[NV],
-                                             double* smem /* NV*NT/32 */, int tid) {
+__device__ __forceinline__ void block_pair_sum(float (&hi)[NV], float (&lo)[NV], float2* smem /* NV*NT/32 */,
+                                               int tid) {
     const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-        float hi = s[v], lo = c[v];
+        float h = hi[v], l = lo[v];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+            const float h2 = __shfl_down_sync(0xffffffffu, h, o), l2 = __shfl_down_sync(0xffffffffu, l, o);
             float t, e;
-            two_sum_f(hi, h2, t, e);
-            hi = t;
-            lo += l2 + e;
+            two_sum_f(h, h2, t, e);
+            h = t;
+            l += l2 + e;
         }
-        if (lane == 0) smem[v * (NT / 32) + warp] = (double)hi + (double)lo;
+        if (lane == 0) smem[v * (NT / 32) + warp] = make_float2(h, l);
     }
     __syncthreads();
     if (tid == 0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            double acc = 0.0;
-            for (int w = 0; w < NT / 32; ++w) acc += smem[v * (NT / 32) + w];
-            val[v] = acc;
+            float2 a = smem[v * (NT / 32)];
+            for (int w = 1; w < NT / 32; ++w) {
+                const float2 b = smem[v * (NT / 32) + w];
+                float t, e;
+                two_sum_f(a.x, b.x, t, e);
+                a = make_float2(t, a.y + b.y + e);
+            }
+            hi[v] = a.x;
+            lo[v] = a.y;
         }
     }
+}
+
+// The same block sum with the result as doubles (thread 0), for finish_reduction.
+template <int NV, int NT>
+__device__ __forceinline__ void block_sum_f2(const float (&s)[NV], const float (&c)[NV], double (&val)[NV],
+                                             double* smem /* NV*NT/32 */, int tid) {
+    float h[NV], l[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        h[v] = s[v];
+        l[v] = c[v];
+    }
+    block_pair_sum<NV, NT>(h, l, reinterpret_cast<float2*>(smem), tid);
+    if (tid == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) val[v] = (double)h[v] + (double)l[v];
+    }
+}
+
+// finish_reduction for float pairs (after block_pair_sum, the pairs valid in thread 0): each
+// block stores its pairs in the 8-byte partial slots, the last block adds them in the fixed
+// order of finish_reduction with TwoSum and block_pair_sum, and thread 0 writes
+// out[v] = hi + lo as a double. Returns true in the block that wrote the result.
+template <int NV, int NT>
+__device__ __forceinline__ bool finish_pair_reduction(const float (&hi)[NV], const float (&lo)[NV], int bid,
+                                                      int nblocks, double* partials, unsigned* counter, double* out,
+                                                      int tid, float2* smem /* NV*NT/32 */) {
+    __shared__ bool last;
+    float2* p = reinterpret_cast<float2*>(partials);
+    __syncthreads();  // smem of block_pair_sum is reused below
+    if (tid == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) p[(int64_t)bid * NV + v] = make_float2(hi[v], lo[v]);
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        last = (t == (unsigned)nblocks - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    float h[NV], l[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        h[v] = 0.f;
+        l[v] = 0.f;
+        for (int b = tid; b < nblocks; b += NT) {
+            const float2 q = __ldcg(p + (int64_t)b * NV + v);
+            float t, e;
+            two_sum_f(h[v], q.x, t, e);
+            h[v] = t;
+            l[v] += q.y + e;
+        }
+    }
+    block_pair_sum<NV, NT>(h, l, smem, tid);
+    if (tid == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[v] = (double)h[v] + (double)l[v];
+        *counter = 0u;
+    }
+    return true;
 }
 
 // Finishes a reduction: block `bid` of `nblocks` stores its NV partials; the last block to

@@ -572,12 +572,12 @@ __global__ void __launch_bounds__(DT) k_oc_vol_bank(int64_t ne, const uint8_t* _
     }
     for (int64_t e = 4 * n4 + t; e < ne; e += stride)
         oc_bank_elem(active[e], frozen[e], x[e], dcx[e], dvx[e], wv[e], bank, rl, move, acc);
-    double v[OC_BANK];
-    float zero[OC_BANK];
+    float lo[OC_BANK];
 #pragma unroll
-    for (int j = 0; j < OC_BANK; ++j) zero[j] = 0.f;
-    block_sum_f2<OC_BANK, DT>(acc, zero, v, sm, threadIdx.x);
-    finish_reduction<OC_BANK, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
+    for (int j = 0; j < OC_BANK; ++j) lo[j] = 0.f;
+    float2* sp = reinterpret_cast<float2*>(sm);
+    block_pair_sum<OC_BANK, DT>(acc, lo, sp, threadIdx.x);
+    finish_pair_reduction<OC_BANK, DT>(acc, lo, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sp);
 }
 
 __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,

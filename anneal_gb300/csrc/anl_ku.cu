@@ -444,15 +444,16 @@ __global__ void __launch_bounds__(KmCfg<T>::NT, KmCfg<T>::MINB) ku_kernel(KuArgs
     }
     if (MODE == KU_APPLY_DOT || (MODE == KU_RESID && std::is_same<T, DF>::value)) {
         const int tid = threadIdx.y * 32 + threadIdx.x;
-        double v[1];
         if constexpr (std::is_same<T, double>::value) {
-            v[0] = dot.value();
+            double v[1] = {dot.value()};
             block_sum<1, NT>(v, sred, tid);
+            finish_reduction<1, NT>(v, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sred);
         } else {
-            const float s1[1] = {dot.a.s}, c1[1] = {dot.a.c};
-            block_sum_f2<1, NT>(s1, c1, v, sred, tid);
+            float h[1] = {dot.a.s}, l[1] = {dot.a.c};
+            float2* sp = reinterpret_cast<float2*>(sred);
+            block_pair_sum<1, NT>(h, l, sp, tid);
+            finish_pair_reduction<1, NT>(h, l, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sp);
         }
-        finish_reduction<1, NT>(v, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sred);
     }
 }
 

@@ -488,10 +488,10 @@ __global__ void __launch_bounds__(NT, 1) kutc_kernel(KuArgs<float> a, KeModal<fl
         tmem_dealloc(tmem, 512);
     }
     if (MODE == KU_APPLY_DOT) {
-        double v[1];
-        const float s1[1] = {dot.a.s}, c1[1] = {dot.a.c};
-        block_sum_f2<1, NT>(s1, c1, v, sred, tid);
-        finish_reduction<1, NT>(v, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sred);
+        float h[1] = {dot.a.s}, l[1] = {dot.a.c};
+        float2* sp = reinterpret_cast<float2*>(sred);
+        block_pair_sum<1, NT>(h, l, sp, tid);
+        finish_pair_reduction<1, NT>(h, l, blockIdx.x, gridDim.x, a.partials, a.counter, a.red_out, tid, sp);
     }
 }
 

@@ -47,22 +47,30 @@ struct Sum<double> {
     __device__ double get() const { return s; }
 };
 
-// block sums of NV accumulators: float-pair trees for the FP32 sums, FP64 trees for FP64 ones
+// Grid sums of NV accumulators into out[0..NV) (finish_reduction's contract; true in the block
+// that wrote them): float-pair trees for the FP32 sums, FP64 trees for FP64 ones. smem holds
+// NV*NT/32 doubles.
 template <int NV, int NT>
-__device__ __forceinline__ void block_sum_of(const Sum<float> (&acc)[NV], double (&v)[NV], double* smem, int tid) {
-    float s[NV], c[NV];
+__device__ __forceinline__ bool finish_sums(const Sum<float> (&acc)[NV], int bid, int nblocks, double* partials,
+                                            unsigned* counter, double* out, double* smem, int tid) {
+    float h[NV], l[NV];
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-        s[i] = acc[i].a.s;
-        c[i] = acc[i].a.c;
+        h[i] = acc[i].a.s;
+        l[i] = acc[i].a.c;
     }
-    block_sum_f2<NV, NT>(s, c, v, smem, tid);
+    float2* sp = reinterpret_cast<float2*>(smem);
+    block_pair_sum<NV, NT>(h, l, sp, tid);
+    return finish_pair_reduction<NV, NT>(h, l, bid, nblocks, partials, counter, out, tid, sp);
 }
 template <int NV, int NT>
-__device__ __forceinline__ void block_sum_of(const Sum<double> (&acc)[NV], double (&v)[NV], double* smem, int tid) {
+__device__ __forceinline__ bool finish_sums(const Sum<double> (&acc)[NV], int bid, int nblocks, double* partials,
+                                            unsigned* counter, double* out, double* smem, int tid) {
+    double v[NV];
 #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = acc[i].get();
     block_sum<NV, NT>(v, smem, tid);
+    return finish_reduction<NV, NT>(v, bid, nblocks, partials, counter, out, tid, smem);
 }
 
 // ------------------------------------------------------------------ masks and levels
@@ -632,14 +640,38 @@ __global__ void k_dot_d(int64_t n, const double* a, const double* b, double* par
     finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
-// x (FP64) -> hi + lo in T
-template <class T>
-__global__ void k_split(int64_t n, const double* x, T* hi, T* lo) {
+// x (FP64) -> hi + lo in two float vectors, without FP64 arithmetic (split_double)
+__global__ void k_split_hl(int64_t n, const double* x, float* hi, float* lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        split_double(x[i], hi[i], lo[i]);
+}
+
+// r = b - y1 - y2 for the FP32 solver, b as float pairs (k_split_df), the differences and
+// ||r||^2 in float-pair arithmetic; sets the CG state as k_true_resid does.
+__global__ void k_true_resid_pair(int64_t n, const DF* b, const float* y1, const float* y2, float* r, PcgScalars* sc,
+                                  int set_state, double* partials, unsigned* counter) {
+    __shared__ double sm[VT / 32];
+    Sum<float> acc[1];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v = x[i];
-        const T h = T(v);
-        hi[i] = h;
-        lo[i] = T(v - (double)h);
+        const DF ri = b[i] - DF(y1[i]) - DF(y2[i]);
+        const float rf = ri.hi + ri.lo;
+        r[i] = rf;
+        acc[0].prod(rf, rf);
+    }
+    __shared__ double res[1];
+    if (finish_sums<1, VT>(acc, blockIdx.x, gridDim.x, partials, counter, res, sm, threadIdx.x)) {
+        if (threadIdx.x == 0) {
+            sc->rr_true = res[0];
+            if (set_state) {
+                sc->rr = res[0];
+                if (!isfinite(res[0])) {
+                    sc->done = 3;
+                    sc->nonfinite = 1;
+                } else {
+                    sc->done = res[0] <= sc->tol2 ? 1 : 0;
+                }
+            }
+        }
     }
 }
 
@@ -760,10 +792,8 @@ __global__ void k_dots_rz_zq(int64_t n, const T* r, const T* z, const T* q, PcgS
             a.prod(r[i], zi);
             if (!rs) b.prod(zi, q[i]);
         });
-    double v[2];
-    block_sum_of<2, VT>(ab, v, sm, threadIdx.x);
     __shared__ double res[2];
-    if (finish_reduction<2, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
+    if (finish_sums<2, VT>(ab, blockIdx.x, gridDim.x, partials, counter, res, sm, threadIdx.x)) {
         if (threadIdx.x == 0) {
             const int it = sc->iters;
             sc->rz[it & 1] = res[0];
@@ -862,10 +892,8 @@ __global__ void k_axpy(int64_t n, const T* p, const T* q, double* x, T* r, PcgSc
                 rr.prod(ri, ri);
             });
     }
-    double v[1];
-    block_sum_of<1, VT>(rr1, v, sm, threadIdx.x);
     __shared__ double res[1];
-    if (finish_reduction<1, VT>(v, blockIdx.x, gridDim.x, partials, counter, res, threadIdx.x, sm)) {
+    if (finish_sums<1, VT>(rr1, blockIdx.x, gridDim.x, partials, counter, res, sm, threadIdx.x)) {
         if (threadIdx.x == 0) {
             sc->alpha = alpha;
             sc->rr = res[0];
@@ -1263,12 +1291,12 @@ static int true_residual(anl_ctx* c, int set_state, cudaStream_t s, bool accurat
     if (!accurate) {
         // plain FP32 evaluation of K x_hi + K x_lo: enough to restart the recurrence, not to
         // certify convergence (its rounding floor is ~eps |K| |dx|)
-        k_split<float><<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (float*)c->xhi, (float*)c->xlo);
+        k_split_hl<<<vgrid(n), VT, 0, s>>>(n, c->xbuf, (float*)c->xhi, (float*)c->xlo);
         ANL_LAUNCH_CHECK();
         ANL_TRY(apply_level<T>(c, L0, (const T*)c->xhi, (T*)c->y1, s));
         ANL_TRY(apply_level<T>(c, L0, (const T*)c->xlo, (T*)c->y2, s));
-        k_true_resid<T><<<vgrid(n), VT, 0, s>>>(n, c->bbuf, (const T*)c->y1, (const T*)c->y2, r, c->sc, set_state,
-                                                c->partials, c->counter);
+        k_true_resid_pair<<<vgrid(n), VT, 0, s>>>(n, (const DF*)c->bdf, (const float*)c->y1, (const float*)c->y2,
+                                                  (float*)r, c->sc, set_state, c->partials, c->counter);
         ANL_LAUNCH_CHECK();
         return ANL_OK;
     }
