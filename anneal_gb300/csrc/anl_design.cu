@@ -502,18 +502,40 @@ int sensitivity(anl_ctx* c, const double* u, int nrhs, const double* coef, const
 // ------------------------------------------------------------------ OC update
 
 // sums over design (active, non-frozen) elements: -dcx, dvx, count
+// a float-pair running sum (TwoSum per term): FP32 instructions only
+struct PairSum {
+    float h = 0.f, l = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float t, e;
+        two_sum_f(h, x, t, e);
+        h = t;
+        l += e;
+    }
+};
+template <int NV>
+__device__ __forceinline__ bool finish_pair_sums(const PairSum (&v)[NV], double* partials, unsigned* counter,
+                                                 double* out, float2* smem) {
+    float h[NV], l[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        h[q] = v[q].h;
+        l[q] = v[q].l;
+    }
+    block_pair_sum<NV, DT>(h, l, smem, threadIdx.x);
+    return finish_pair_reduction<NV, DT>(h, l, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, smem);
+}
+
 __global__ void k_oc_scale(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* dcx, const float* dvx,
                            double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[3 * DT / 32];
-    double v[3] = {0, 0, 0};
+    __shared__ float2 sm[3 * DT / 32];
+    PairSum v[3];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
         if (active[e] && !frozen[e]) {
-            v[0] -= dcx[e];
-            v[1] += dvx[e];
-            v[2] += 1.0;
+            v[0].add(-dcx[e]);
+            v[1].add(dvx[e]);
+            v[2].add(1.f);
         }
-    block_sum<3, DT>(v, sm, threadIdx.x);
-    finish_reduction<3, DT>(v, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
+    finish_pair_sums<3>(v, partials, counter, out, sm);
 }
 
 // With no projection the volume is linear in xn: vol = sum_j wv_j xn_j + sum_frozen phi,
@@ -582,15 +604,14 @@ __global__ void __launch_bounds__(DT) k_oc_vol_bank(int64_t ne, const uint8_t* _
 
 __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,
                              double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[DT / 32];
-    double f[1] = {0.0};
+    __shared__ float2 sm[DT / 32];
+    PairSum f[1];
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
         const bool a = active[e] != 0, fz = frozen[e] != 0;
         v[e] = a && !fz ? phi[e] : 0.f;
-        if (a && fz) f[0] += phi[e];
+        if (a && fz) f[0].add(phi[e]);
     }
-    block_sum<1, DT>(f, sm, threadIdx.x);
-    finish_reduction<1, DT>(f, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
+    finish_pair_sums<1>(f, partials, counter, out, sm);
 }
 
 __global__ void k_oc_final(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x, const float* dcx,
@@ -725,66 +746,78 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
 
 __global__ void k_stats(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* xold, const float* xnew,
                         const float* xphys, const float* phi, double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[4 * DT / 32];
+    // grey count, design count, volume as float-pair sums; the largest change as a fifth
+    // partial (a maximum is exact in any order), carried as the pair (max, 0)
+    __shared__ float2 sm[4 * DT / 32];
+    __shared__ float smax[DT / 32];
     __shared__ bool last;
-    double v[4] = {0, 0, 0, 0};   // grey count, design count, volume, max change
+    PairSum v[3];
+    float mx = 0.f;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
         if (!active[e]) continue;
         const float xp = xphys[e];
-        v[2] += (double)phi[e] * (double)xp;
+        float pv, pe;
+        two_prod(phi[e], xp, pv, pe);  // the exact product as a pair
+        v[2].add(pv);
+        v[2].add(pe);
         if (!frozen[e]) {
-            v[3] = fmax(v[3], (double)fabsf(xnew[e] - xold[e]));
-            if (xp > 0.1f && xp < 0.9f) v[0] += 1.0;
-            v[1] += 1.0;
+            mx = fmaxf(mx, fabsf(xnew[e] - xold[e]));
+            if (xp > 0.1f && xp < 0.9f) v[0].add(1.f);
+            v[1].add(1.f);
         }
     }
-    // block: sums for 0..2, max for 3 (exact in any order)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int q = 0; q < 4; ++q) {
-        double x = v[q];
-        for (int o = 16; o > 0; o >>= 1) {
-            const double y = __shfl_down_sync(0xffffffffu, x, o);
-            x = q == 3 ? fmax(x, y) : x + y;
-        }
-        if (lane == 0) sm[q * (DT / 32) + warp] = x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if (lane == 0) smax[warp] = mx;
+    float h[3], l[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        h[q] = v[q].h;
+        l[q] = v[q].l;
     }
-    __syncthreads();
+    block_pair_sum<3, DT>(h, l, sm, threadIdx.x);  // its barrier also publishes smax
+    float2* p = reinterpret_cast<float2*>(partials);
     if (threadIdx.x == 0) {
-        for (int q = 0; q < 4; ++q) {
-            double x = q == 3 ? 0.0 : 0.0;
-            for (int w = 0; w < DT / 32; ++w) x = q == 3 ? fmax(x, sm[q * (DT / 32) + w]) : x + sm[q * (DT / 32) + w];
-            partials[(int64_t)blockIdx.x * 4 + q] = x;
-        }
+        float m = 0.f;
+        for (int w = 0; w < DT / 32; ++w) m = fmaxf(m, smax[w]);
+        for (int q = 0; q < 3; ++q) p[(int64_t)blockIdx.x * 4 + q] = make_float2(h[q], l[q]);
+        p[(int64_t)blockIdx.x * 4 + 3] = make_float2(m, 0.f);
         __threadfence();
         last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double a[4] = {0, 0, 0, 0};
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += DT)
-        for (int q = 0; q < 4; ++q) {
-            const double x = __ldcg(partials + (int64_t)b * 4 + q);
-            a[q] = q == 3 ? fmax(a[q], x) : a[q] + x;
-        }
-    __syncthreads();
-    for (int q = 0; q < 4; ++q) {
-        double x = a[q];
-        for (int o = 16; o > 0; o >>= 1) {
-            const double y = __shfl_down_sync(0xffffffffu, x, o);
-            x = q == 3 ? fmax(x, y) : x + y;
-        }
-        if (lane == 0) sm[q * (DT / 32) + warp] = x;
+    float m = 0.f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        h[q] = 0.f;
+        l[q] = 0.f;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double r[4];
-        for (int q = 0; q < 4; ++q) {
-            double x = 0.0;
-            for (int w = 0; w < DT / 32; ++w) x = q == 3 ? fmax(x, sm[q * (DT / 32) + w]) : x + sm[q * (DT / 32) + w];
-            r[q] = x;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += DT) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float2 x = __ldcg(p + (int64_t)b * 4 + q);
+            float t, e;
+            two_sum_f(h[q], x.x, t, e);
+            h[q] = t;
+            l[q] += x.y + e;
         }
-        out[0] = r[3];
+        m = fmaxf(m, __ldcg(p + (int64_t)b * 4 + 3).x);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    __syncthreads();
+    if (lane == 0) smax[warp] = m;
+    block_pair_sum<3, DT>(h, l, sm, threadIdx.x);
+    if (threadIdx.x == 0) {
+        float mm = 0.f;
+        for (int w = 0; w < DT / 32; ++w) mm = fmaxf(mm, smax[w]);
+        double r[3];
+        for (int q = 0; q < 3; ++q) r[q] = (double)h[q] + (double)l[q];
+        // change, grey fraction of the design elements, volume, design element count
+        out[0] = mm;
         out[1] = r[1] > 0 ? r[0] / r[1] : 0.0;
         out[2] = r[2];
         out[3] = r[1];
