@@ -238,6 +238,9 @@ static void free_ctx(anl_ctx* c) {
     f(c->Ainv);
     f(c->ainv_hi);
     f(c->sens_df);
+    f(c->oc_el);
+    f(c->oc_gw);
+    f(c->oc_state);
     f(c->ainv_lo);
     f(c->flag_d);
     f(c->restart_d);

@@ -299,7 +299,7 @@ struct RedScratch {
     int max_vals;
 };
 
-constexpr int kMaxRedVals = 8;
+constexpr int kMaxRedVals = 16;
 constexpr int kRedBlocks = 1216;  // 152 SMs x 8: grid of the grid-stride vector kernels
 
 // Sum of `val` over the block, for NV values; result valid in the thread with flat index 0.

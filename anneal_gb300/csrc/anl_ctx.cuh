@@ -103,6 +103,12 @@ struct anl_ctx {
     anl::PcgScalars* sc_base = nullptr;
     anl::DF* sens_df = nullptr;  // the sensitivity's displacements as float pairs (grows)
     size_t sens_df_cap = 0;
+    float4* oc_el = nullptr;     // the OC update's lambda-free element data (grows)
+    size_t oc_el_cap = 0;
+    float2* oc_gw = nullptr;
+    size_t oc_gw_cap = 0;
+    double* oc_state = nullptr;  // the OC bisection's device state (OcState, anl_design.cu)
+    size_t oc_state_cap = 0;
     float* ainv_hi = nullptr;  // the coarsest dense inverse as float pairs (the tail's coarse solve)
     float* ainv_lo = nullptr;
 #ifndef ANL_CHEB_LO

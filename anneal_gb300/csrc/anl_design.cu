@@ -4,6 +4,7 @@
 // Element fields are FP32 on the full grid (x fastest, zero on inactive elements); sums
 // that decide the OC bisection and the history values accumulate in FP64.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <vector>
 
@@ -143,6 +144,16 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
     const bool in_xy = i < d.nx && j < d.ny;
     double vol = 0.0;
     for (int k = kb; k < kend; ++k) {
+        // this layer's epilogue inputs, loaded before the barrier so their latency overlaps it
+        const int64_t e = in_xy ? d.elem(i, j, k) : 0;
+        bool act = false, fzn = false;
+        float hs = 1.f, ph = 0.f;
+        if (in_xy) {
+            act = a.active[e] != 0;
+            if (MODE == F_FWD || MODE == F_PHYS || MODE == F_OCVOL) hs = a.Hs[e];
+            if (MODE == F_PHYS || MODE == F_OCVOL) fzn = a.frozen[e] != 0;
+            if (MODE == F_OCVOL) ph = a.phi[e];
+        }
         if (RT == 1) {  // plane k + 1 was loaded during the previous layer; load plane k + 2
             commit(k + 1);
             if (k + 1 < kend) prefetch(k + 2);
@@ -171,24 +182,22 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
                     }
                 }
             }
-            const int64_t e = d.elem(i, j, k);
-            const bool act = a.active[e] != 0;
             if (MODE == F_HS) {
                 a.out[e] = s == 0.f ? 1.f : s;
             } else if (MODE == F_FWD) {
-                a.out[e] = act ? s / a.Hs[e] : 0.f;
+                a.out[e] = act ? s / hs : 0.f;
             } else if (MODE == F_BWD) {
                 a.out[e] = act ? s : 0.f;
             } else {
                 // physical(): projection (optimize.py:81-87), frozen -> 1 (optimize.py:92)
-                float xt = act ? s / a.Hs[e] : 0.f;
+                float xt = act ? s / hs : 0.f;
                 float xp = xt, g = 1.f;
                 if (a.beta > 0.f) {
                     const float th = tanhf(a.beta * (xt - a.eta));
                     xp = (a.t0 + th) / (a.t0 + a.t1);
                     g = a.beta * (1.f - th * th) / (a.t0 + a.t1);
                 }
-                if (a.frozen[e]) xp = 1.f;
+                if (fzn) xp = 1.f;
                 if (!act) {
                     xp = 0.f;
                     g = 0.f;
@@ -197,7 +206,7 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
                     a.out[e] = xp;
                     if (a.dxp) a.dxp[e] = g;
                 } else {
-                    vol += act ? (double)a.phi[e] * (double)xp : 0.0;
+                    vol += act ? (double)ph * (double)xp : 0.0;
                 }
             }
         }
@@ -542,64 +551,172 @@ __global__ void k_oc_scale(int64_t ne, const uint8_t* active, const uint8_t* fro
 // wv = Filter.backward(phi on non-frozen elements). One pass evaluates a bank of up to OC_BANK
 // lambdas, the nodes of OC_BANK_DEPTH consecutive bisection steps; each volume is its own
 // deterministic two-stage sum, so the bisection takes the decisions a pass per step would.
-constexpr int OC_BANK_DEPTH = 3;
+// The part of each element's update that does not depend on lambda is formed once per OC
+// update (k_oc_prep): (s, dvx, lo, hi) and (g, w), with g the value where dvx lambda underflows
+// (hi if the element grows, else lo), frozen elements as lo = hi = 1 and inactive ones with w = 0.
+// A pass then costs a multiply, a compare, a clamp and a multiply-add per lambda and element.
+constexpr int OC_BANK_DEPTH = 4;
 constexpr int OC_BANK = (1 << OC_BANK_DEPTH) - 1;
 static_assert(OC_BANK <= kMaxRedVals, "one partial per lambda and block");
+static_assert(OC_BANK <= 16, "the bank's volumes fit red_out");
 struct OcBank {
     float lam[OC_BANK];
     int n;
 };
 
-// One element of the bank pass: adds w * xn(lambda_j) to acc[j] for every lambda of the bank.
-__device__ __forceinline__ void oc_bank_elem(bool act, bool fz, float x, float dcx, float dvx, float w,
-                                             const OcBank& bank, const float (&rl)[OC_BANK], float move,
-                                             float (&acc)[OC_BANK]) {
-    if (!act) return;
-    const OcElem o = oc_elem(x, dcx, dvx, move);
-#pragma unroll
-    for (int j = 0; j < OC_BANK; ++j)
-        if (j < bank.n) acc[j] = fmaf(w, fz ? 1.f : oc_xn(o, bank.lam[j], rl[j]), acc[j]);
+__global__ void k_oc_prep(int64_t ne, const uint8_t* __restrict__ active, const uint8_t* __restrict__ frozen,
+                          const float* __restrict__ x, const float* __restrict__ dcx, const float* __restrict__ dvx,
+                          const float* __restrict__ wv, float move, float4* __restrict__ el, float2* __restrict__ gw) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        if (!active[e]) {
+            el[e] = make_float4(0.f, 1.f, 0.f, 0.f);
+            gw[e] = make_float2(0.f, 0.f);
+        } else if (frozen[e]) {
+            el[e] = make_float4(0.f, 1.f, 1.f, 1.f);
+            gw[e] = make_float2(1.f, wv[e]);
+        } else {
+            const OcElem o = oc_elem(x[e], dcx[e], dvx[e], move);
+            el[e] = make_float4(o.s, o.dvx, o.lo, o.hi);
+            gw[e] = make_float2(o.grows ? o.hi : o.lo, wv[e]);
+        }
+    }
 }
 
-// Each thread takes groups of 4 consecutive elements (16-byte loads when every array is
-// aligned; the host checks), with every load of a group issued before any is used. A thread
-// adds its ~14 elements per lambda in FP32 in a fixed order; blocks and the grid add in FP64.
-template <bool VEC>
-__global__ void __launch_bounds__(DT) k_oc_vol_bank(int64_t ne, const uint8_t* __restrict__ active,
-                                                    const uint8_t* __restrict__ frozen, const float* __restrict__ x,
-                                                    const float* __restrict__ dcx, const float* __restrict__ dvx,
-                                                    const float* __restrict__ wv, OcBank bank, float move,
+// One element of the bank pass: adds w * xn(lambda_j) to acc[j] for every lambda of the bank.
+// Each thread takes its elements in grid-stride order and adds them per lambda in FP32 in a
+// fixed order; blocks and the grid add in float pairs.
+// The bisection's state in device memory: the passes, the decisions between them and the final
+// update run back to back on the stream with no host round trip (optimize.py:147-160).
+struct OcState {
+    double lo, hi, lam;
+    double vfrozen, vtarget;
+    int steps, stop;
+    OcBank bank;            // the lambdas of the next pass (FP32, as the passes use them)
+    double lamd[OC_BANK];   // the same lambdas in FP64: the decisions' sqrt(lo hi)
+};
+
+// The bank of the next OC_BANK_DEPTH (at most 100 - steps) bisection steps from [lo, hi], by one
+// warp: level by level of the bisection tree (node j of the in-order numbering), the nodes of a
+// level in parallel lanes, so the FP64 square roots (slow on this part) form a chain of `depth`.
+// Each node's value is sqrt(l h) of its interval, as the bisection forms it.
+__device__ void oc_make_bank(OcState* st, int lane) {
+    __shared__ double L[OC_BANK], H[OC_BANK];
+    const int depth = min(OC_BANK_DEPTH, 100 - st->steps);
+    const int nodes = (1 << depth) - 1, root = (1 << (depth - 1)) - 1;
+    if (lane == 0) {
+        L[root] = st->lo;
+        H[root] = st->hi;
+        st->bank.n = nodes;
+    }
+    __syncwarp();
+    for (int level = 0; level < depth; ++level) {
+        const int half = 1 << (depth - 1 - level);
+        const int j = half - 1 + lane * 2 * half;
+        if (lane < (1 << level)) {
+            const double t = sqrt(L[j] * H[j]);
+            st->lamd[j] = t;
+            st->bank.lam[j] = (float)t;
+            if (level + 1 < depth) {
+                L[j - half / 2] = L[j];
+                H[j - half / 2] = t;
+                L[j + half / 2] = t;
+                H[j + half / 2] = H[j];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// one warp
+__global__ void k_oc_begin(OcState* st, const double* sums, const double* vfrozen, double vtarget) {
+    if (threadIdx.x == 0) {
+        // optimize.py:145: the bracket from the mean sensitivities of the design elements
+        double scale = 1.0;
+        const double nd = sums[2];
+        if (nd > 0) {
+            const double mdc = sums[0] / nd, mdv = sums[1] / nd;
+            scale = fmax(mdc / fmax(mdv, 1e-30), 1e-300);
+        }
+        st->lo = scale * 1e-8;
+        st->hi = scale * 1e8;
+        st->lam = sqrt(st->lo * st->hi);
+        st->vfrozen = vfrozen ? *vfrozen : 0.0;
+        st->vtarget = vtarget;
+        st->steps = 0;
+        st->stop = 0;
+    }
+    __syncwarp();
+    oc_make_bank(st, threadIdx.x);
+}
+
+// one warp: the bank's steps, one per level of the tree (optimize.py:147-160), then the next bank
+__global__ void k_oc_decide(OcState* st, const double* vols) {
+    if (st->stop) return;  // the same for every lane
+    if (threadIdx.x == 0) {
+        const int depth = min(OC_BANK_DEPTH, 100 - st->steps);
+        int idx = (1 << (depth - 1)) - 1, step = depth >= 2 ? 1 << (depth - 2) : 0;
+        double lo = st->lo, hi = st->hi, lam = st->lam;
+        for (int d = 0; d < depth; ++d) {
+            lam = st->lamd[idx];  // sqrt(lo hi) of the current bracket
+            const double vol = vols[idx] + st->vfrozen;
+            if (vol > st->vtarget) {
+                lo = lam;
+                idx += step;
+            } else {
+                hi = lam;
+                idx -= step;
+            }
+            step >>= 1;
+            ++st->steps;
+            if (hi / lo < 1 + 1e-9) {
+                st->stop = 1;
+                break;
+            }
+        }
+        st->lo = lo;
+        st->hi = hi;
+        st->lam = lam;
+        if (st->steps >= 100) st->stop = 1;
+    }
+    __syncwarp();
+    if (!st->stop) oc_make_bank(st, threadIdx.x);
+}
+
+constexpr int OCB_T = 512;  // threads of a bank pass: two CTAs per SM, each thread ~27 elements at 12.8M DOF
+__global__ void __launch_bounds__(OCB_T, 2) k_oc_vol_bank(int64_t ne, const float4* __restrict__ el,
+                                                    const float2* __restrict__ gw, const OcState* st,
                                                     double* partials, unsigned* counter, double* out) {
-    __shared__ double sm[OC_BANK * DT / 32];
+    if (st->stop) return;  // the same for every block
+    const OcBank bank = st->bank;
+    __shared__ float2 sm[OC_BANK * OCB_T / 32];
     float acc[OC_BANK], rl[OC_BANK];
 #pragma unroll
     for (int j = 0; j < OC_BANK; ++j) {
         acc[j] = 0.f;
         rl[j] = oc_rl(bank.lam[j]);
     }
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x, t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t n4 = VEC ? ne >> 2 : 0;
-    for (int64_t g = t; g < n4; g += stride) {
-        const int64_t e = 4 * g;
-        const uchar4 a4 = *reinterpret_cast<const uchar4*>(active + e);
-        const uchar4 f4 = *reinterpret_cast<const uchar4*>(frozen + e);
-        const float4 x4 = *reinterpret_cast<const float4*>(x + e);
-        const float4 c4 = *reinterpret_cast<const float4*>(dcx + e);
-        const float4 v4 = *reinterpret_cast<const float4*>(dvx + e);
-        const float4 w4 = *reinterpret_cast<const float4*>(wv + e);
-        oc_bank_elem(a4.x, f4.x, x4.x, c4.x, v4.x, w4.x, bank, rl, move, acc);
-        oc_bank_elem(a4.y, f4.y, x4.y, c4.y, v4.y, w4.y, bank, rl, move, acc);
-        oc_bank_elem(a4.z, f4.z, x4.z, c4.z, v4.z, w4.z, bank, rl, move, acc);
-        oc_bank_elem(a4.w, f4.w, x4.w, c4.w, v4.w, w4.w, bank, rl, move, acc);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += 2 * stride) {
+        // two elements per iteration, their loads issued before either is used
+        const bool two = e + stride < ne;
+        const float4 q0 = el[e];
+        const float2 t0 = gw[e];
+        const float4 q1 = two ? el[e + stride] : make_float4(0.f, 1.f, 0.f, 0.f);
+        const float2 t1 = two ? gw[e + stride] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < OC_BANK; ++j) {
+            if (j < bank.n) {  // oc_xn with the elements' lambda-free parts
+                const float v0 = q0.y * bank.lam[j] > 1e-30f ? fminf(fmaxf(q0.x * rl[j], q0.z), q0.w) : t0.x;
+                const float v1 = q1.y * bank.lam[j] > 1e-30f ? fminf(fmaxf(q1.x * rl[j], q1.z), q1.w) : t1.x;
+                acc[j] = fmaf(t1.y, v1, fmaf(t0.y, v0, acc[j]));
+            }
+        }
     }
-    for (int64_t e = 4 * n4 + t; e < ne; e += stride)
-        oc_bank_elem(active[e], frozen[e], x[e], dcx[e], dvx[e], wv[e], bank, rl, move, acc);
     float lo[OC_BANK];
 #pragma unroll
     for (int j = 0; j < OC_BANK; ++j) lo[j] = 0.f;
-    float2* sp = reinterpret_cast<float2*>(sm);
-    block_pair_sum<OC_BANK, DT>(acc, lo, sp, threadIdx.x);
-    finish_pair_reduction<OC_BANK, DT>(acc, lo, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sp);
+    block_pair_sum<OC_BANK, OCB_T>(acc, lo, sm, threadIdx.x);
+    finish_pair_reduction<OC_BANK, OCB_T>(acc, lo, blockIdx.x, gridDim.x, partials, counter, out, threadIdx.x, sm);
 }
 
 __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* phi, float* v,
@@ -615,7 +732,8 @@ __global__ void k_oc_weights(int64_t ne, const uint8_t* active, const uint8_t* f
 }
 
 __global__ void k_oc_final(int64_t ne, const uint8_t* active, const uint8_t* frozen, const float* x, const float* dcx,
-                           const float* dvx, float lam, float move, float* xnew) {
+                           const float* dvx, const OcState* st, float move, float* xnew) {
+    const float lam = (float)st->lam;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x)
         xnew[e] = active[e] ? (frozen[e] ? 1.f : oc_xn(x[e], dcx[e], dvx[e], lam, move)) : 0.f;
 }
@@ -630,115 +748,101 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
               double move, double beta, double eta, double vtarget, float* xnew, int* steps_out, double* lam_out,
               cudaStream_t s) {
     const int64_t ne = c->d.ne();
+    ANL_TRY(grow(c->oc_state, c->oc_state_cap, 1, sizeof(OcState)));
+    OcState* st = reinterpret_cast<OcState*>(c->oc_state);
     k_oc_scale<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, dcx, dvx, c->partials, c->counter, c->red_out);
     ANL_LAUNCH_CHECK();
-    ANL_TRY(read_red(c, 3, s));
-    // optimize.py:145
-    double scale = 1.0;
-    const double nd = c->red_h[2];
-    if (nd > 0) {
-        const double mdc = c->red_h[0] / nd, mdv = c->red_h[1] / nd;
-        scale = std::max(mdc / std::max(mdv, 1e-30), 1e-300);
-    }
-    double lo = scale * 1e-8, hi = scale * 1e8;
     const double mv = beta <= 1 ? move : move / 2;  // optimize.py:151
-    double vfrozen = 0.0;
     const bool linear = !(beta > 0);
     if (linear) {
-        k_oc_weights<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, phi, c->ftmp2, c->partials, c->counter, c->red_out);
+        // With no projection the volume is linear in xn (see k_oc_vol_bank): frozen volume and
+        // the filtered weights, the lambda-free element data, then the passes, each followed by
+        // its decisions, on the device; one synchronisation at the end
+        k_oc_weights<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, phi, c->ftmp2, c->partials, c->counter,
+                                              c->red_out + 8);
         ANL_LAUNCH_CHECK();
-        ANL_TRY(read_red(c, 1, s));
-        vfrozen = c->red_h[0];
+        k_oc_begin<<<1, 32, 0, s>>>(st, c->red_out, c->red_out + 8, vtarget);
+        ANL_LAUNCH_CHECK();
         ANL_TRY(filter_apply(c, false, c->ftmp2, c->ftmp, s));
-    }
-    double lam = std::sqrt(lo * hi);
-    int steps = 0;
-    // linear volume: OC_BANK_DEPTH bisection steps per pass over the design
-    const bool vec = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(dcx) |
-                       reinterpret_cast<uintptr_t>(dvx) | reinterpret_cast<uintptr_t>(c->ftmp)) & 15) == 0 &&
-                     ((reinterpret_cast<uintptr_t>(c->active) | reinterpret_cast<uintptr_t>(frozen)) & 3) == 0;
-    while (linear && steps < 100) {
-        const int depth = std::min(OC_BANK_DEPTH, 100 - steps);
-        const int nodes = (1 << depth) - 1, root = (1 << (depth - 1)) - 1;
-        OcBank bank{};
-        bank.n = nodes;
-        for (int j = 0; j < nodes; ++j) {  // node j (in order): lambda on the path from the root
-            double l = lo, h = hi;
-            int idx = root, step = depth >= 2 ? 1 << (depth - 2) : 0;
-            while (true) {
-                const double t = std::sqrt(l * h);
-                if (j == idx) {
-                    bank.lam[j] = (float)t;
-                    break;
-                }
-                if (j > idx) {
-                    l = t;
-                    idx += step;
-                } else {
-                    h = t;
-                    idx -= step;
-                }
-                step >>= 1;
-            }
-        }
-        if (vec)
-            k_oc_vol_bank<true><<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, c->ftmp, bank, (float)mv,
-                                                         c->partials, c->counter, c->red_out);
-        else
-            k_oc_vol_bank<false><<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, c->ftmp, bank,
-                                                          (float)mv, c->partials, c->counter, c->red_out);
+        ANL_TRY(grow(c->oc_el, c->oc_el_cap, (size_t)ne, sizeof(float4)));
+        ANL_TRY(grow(c->oc_gw, c->oc_gw_cap, (size_t)ne, sizeof(float2)));
+        k_oc_prep<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, c->ftmp, (float)mv, c->oc_el,
+                                           c->oc_gw);
         ANL_LAUNCH_CHECK();
-        ANL_TRY(read_red(c, nodes, s));
-        bool stop = false;
-        int idx = root, step = depth >= 2 ? 1 << (depth - 2) : 0;
-        for (int d = 0; d < depth; ++d) {  // optimize.py:147-160, one step per level of the bank
-            lam = std::sqrt(lo * hi);
-            const double vol = c->red_h[idx] + vfrozen;
-            if (vol > vtarget) {
-                lo = lam;
-                idx += step;
-            } else {
-                hi = lam;
-                idx -= step;
-            }
-            step >>= 1;
-            ++steps;
-            if (hi / lo < 1 + 1e-9) {
-                stop = true;
-                break;
-            }
+        // the bracket ratio starts at 1e16 and is square-rooted by every step: 36 steps reach
+        // 1 + 1e-9; passes for 40, then more only if the state has not stopped (never seen)
+        int passes = (40 + OC_BANK_DEPTH - 1) / OC_BANK_DEPTH;
+        static int sms = 0;
+        if (sms == 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         }
-        if (stop) break;
+        const int bank_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(2 * sms, (ne + OCB_T - 1) / OCB_T));
+        for (int round = 0; round < 100 / OC_BANK_DEPTH + 1; ++round) {
+            for (int q = 0; q < passes; ++q) {
+                k_oc_vol_bank<<<bank_blocks, OCB_T, 0, s>>>(ne, c->oc_el, c->oc_gw, st, c->partials, c->counter,
+                                                            c->red_out);
+                ANL_LAUNCH_CHECK();
+                k_oc_decide<<<1, 32, 0, s>>>(st, c->red_out);
+                ANL_LAUNCH_CHECK();
+            }
+            ANL_CUDA(cudaMemcpyAsync(c->red_h, st, offsetof(OcState, bank), cudaMemcpyDeviceToHost, s));
+            ANL_CUDA(cudaStreamSynchronize(s));
+            if (reinterpret_cast<const OcState*>(c->red_h)->stop) break;
+            passes = 1;
+        }
+    } else {
+        ANL_TRY(read_red(c, 3, s));
+        double scale = 1.0;  // optimize.py:145
+        const double nd = c->red_h[2];
+        if (nd > 0) {
+            const double mdc = c->red_h[0] / nd, mdv = c->red_h[1] / nd;
+            scale = std::max(mdc / std::max(mdv, 1e-30), 1e-300);
+        }
+        double lo = scale * 1e-8, hi = scale * 1e8, lam = std::sqrt(lo * hi);
+        int steps = 0;
+        for (int k = 0; k < 100; ++k) {  // projected volume: one filter pass per step
+            lam = std::sqrt(lo * hi);
+            FilterArgs a{};
+            a.frozen = frozen;
+            a.beta = (float)beta;
+            a.eta = (float)eta;
+            a.t0 = (float)std::tanh(beta * eta);
+            a.t1 = (float)std::tanh(beta * (1 - eta));
+            a.x = x;
+            a.dcx = dcx;
+            a.dvx = dvx;
+            a.phi = phi;
+            a.lam = (float)lam;
+            a.move = (float)mv;
+            a.partials = c->partials;
+            a.counter = c->counter;
+            a.red_out = c->red_out;
+            ANL_TRY(launch_filter(c, F_OCVOL, a, s));
+            ANL_TRY(read_red(c, 1, s));
+            const double vol = c->red_h[0];
+            if (vol > vtarget) lo = lam;
+            else hi = lam;
+            ++steps;
+            if (hi / lo < 1 + 1e-9) break;
+        }
+        OcState* h = reinterpret_cast<OcState*>(c->red_h);  // pinned; its head fields only
+        h->lo = lo;
+        h->hi = hi;
+        h->lam = lam;
+        h->vfrozen = 0.0;
+        h->vtarget = vtarget;
+        h->steps = steps;
+        h->stop = 1;
+        ANL_CUDA(cudaMemcpyAsync(st, h, offsetof(OcState, bank), cudaMemcpyHostToDevice, s));
+        ANL_CUDA(cudaStreamSynchronize(s));
     }
-    for (int k = 0; k < 100 && !linear; ++k) {  // projected volume: one filter pass per step
-        lam = std::sqrt(lo * hi);
-        FilterArgs a{};
-        a.frozen = frozen;
-        a.beta = (float)beta;
-        a.eta = (float)eta;
-        a.t0 = (float)std::tanh(beta * eta);
-        a.t1 = (float)std::tanh(beta * (1 - eta));
-        a.x = x;
-        a.dcx = dcx;
-        a.dvx = dvx;
-        a.phi = phi;
-        a.lam = (float)lam;
-        a.move = (float)mv;
-        a.partials = c->partials;
-        a.counter = c->counter;
-        a.red_out = c->red_out;
-        ANL_TRY(launch_filter(c, F_OCVOL, a, s));
-        ANL_TRY(read_red(c, 1, s));
-        const double vol = c->red_h[0];
-        if (vol > vtarget) lo = lam;
-        else hi = lam;
-        ++steps;
-        if (hi / lo < 1 + 1e-9) break;
-    }
-    k_oc_final<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, (float)lam, (float)mv, xnew);
+    k_oc_final<<<dgrid(ne), DT, 0, s>>>(ne, c->active, frozen, x, dcx, dvx, st, (float)mv, xnew);
     ANL_LAUNCH_CHECK();
-    if (steps_out) *steps_out = steps;
-    if (lam_out) *lam_out = lam;
+    const OcState& r = *reinterpret_cast<const OcState*>(c->red_h);
+    if (steps_out) *steps_out = r.steps;
+    if (lam_out) *lam_out = r.lam;
     return ANL_OK;
 }
 

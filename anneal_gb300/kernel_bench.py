@@ -3,11 +3,15 @@
     python -m anneal_gb300.kernel_bench [--shape NX NY NZ] [--reps R] [--fp64]
     python -m anneal_gb300.kernel_bench --export [--shape NX NY NZ] [--reps R]
     python -m anneal_gb300.kernel_bench --voxel [--shape NX NY NZ] [--reps R] [--subdiv N]
+    python -m anneal_gb300.kernel_bench --simp [--scale S] [--reps R] [--six]
 
 --export times the iso-surface export instead: zoom (x2), classify, scan, emit, 10 Taubin
 steps and the component labels on a smooth synthetic density field.
 --voxel times the voxeliser (s = 3) on a sphere of 20 * 4^subdiv triangles filling most of the
 grid's short side (h = 1) plus a rotated box.
+--simp runs R SIMP iterations of the L-bracket (scale S: 1 is 192x96x96, 4/3 the 256x128x128
+bench workload; --six: the six-load-case variant) on the FP32 path and prints their wall times
+and CG iterations (a driver for profiling the kernels of a SIMP step).
 
 Prints one JSON line: milliseconds per launch (CUDA events, after warm-up), the
 algorithmic bytes (24 per node + 4 per element: read u, write y, read the element
@@ -35,7 +39,12 @@ def main():
     ap.add_argument("--voxel", action="store_true")
     ap.add_argument("--subdiv", type=int, default=6)
     ap.add_argument("--tc", action="store_true", help="the tensor-core K u kernel (FP32)")
+    ap.add_argument("--simp", action="store_true")
+    ap.add_argument("--scale", type=float, default=4.0 / 3.0)
+    ap.add_argument("--six", action="store_true")
     a = ap.parse_args()
+    if a.simp:
+        return simp_bench(a.scale, a.reps, a.six)
     if a.tc:
         import os
         os.environ["ANL_TC"] = "1"
@@ -128,6 +137,28 @@ def voxel_bench(shape, reps, subdiv):
                       "pairs": vox.pairs, "crossings": vox.hits, "ms_per_call": ms,
                       "elements_per_s": ne / (ms * 1e-3), "fill_sum": float(f.sum())}))
     vox.close()
+
+
+def simp_bench(scale, reps, six):
+    import time
+    from . import optimize as O, problems as P
+    from .fem import Grid
+    w = (P.six_case_bracket if six else P.lbracket)(scale=scale, vf=0.25, r_vox=2.0, emin=1e-9)
+    O.EMIN = 1e-9
+    run = O.SimpRunner(Grid(w.shape, 1.0, (0.0, 0.0, 0.0)), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights,
+                       w.E0, w.nu, w.vf, iters=max(reps, 1), r_mm=w.r_vox, x0=np.full(w.nelem, w.vf), beta_max=0.0,
+                       log=lambda *a: None, precision="fp32")
+    ms, cg = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = run.step()
+        torch.cuda.synchronize()
+        ms.append(1e3 * (time.perf_counter() - t0))
+        cg.append(h["cgIters"])
+    print(json.dumps({"workload": f"{'sixcase' if six else 'lbracket'}-{w.shape[0]}x{w.shape[1]}x{w.shape[2]}",
+                      "ms_per_iteration": ms, "cg_iters": cg}))
+    run.close()
 
 
 if __name__ == "__main__":
