@@ -430,14 +430,26 @@ __global__ void __launch_bounds__(KmCfg<T>::NT, KmCfg<T>::MINB) ku_kernel(KuArgs
         int64_t n = t.n0 + (int64_t)(k0 - 1) * t.plane;  // node (ie, je, kk)
         t.epi_load(n, false, EA);
         __syncthreads();  // slot of layer k0-2 is read before the loop refills it
-        for (int kk = k0 - 1; kk < kend; kk += 2) {
-            t.step(kk, kend, kk >= k0, n, par, A, B, EA, EB, dot);
-            par ^= 1;
-            n += t.plane;
-            if (kk + 1 >= kend) break;
-            t.step(kk + 1, kend, true, n, par, B, A, EB, EA, dot);
-            par ^= 1;
-            n += t.plane;
+        if constexpr (std::is_same<T, DF>::value) {
+            // one step per trip and the carries copied: the pair arithmetic of a step is long
+            // enough that a second inlined copy of it overflows the instruction cache
+            for (int kk = k0 - 1; kk < kend; ++kk) {
+                t.step(kk, kend, kk >= k0, n, par, A, B, EA, EB, dot);
+                par ^= 1;
+                n += t.plane;
+                A = B;
+                EA = EB;
+            }
+        } else {
+            for (int kk = k0 - 1; kk < kend; kk += 2) {
+                t.step(kk, kend, kk >= k0, n, par, A, B, EA, EB, dot);
+                par ^= 1;
+                n += t.plane;
+                if (kk + 1 >= kend) break;
+                t.step(kk + 1, kend, true, n, par, B, A, EB, EA, dot);
+                par ^= 1;
+                n += t.plane;
+            }
         }
         cp_async_wait<0>();
         __syncthreads();  // the ring is idle before the next segment restages it

@@ -8,7 +8,9 @@ displacement, sensitivity, two filter backward passes, OC bisection, history val
 
 After W warm-up steps, K device-timed steps (design resident in HBM) alternate with K
 end-to-end steps (design copied host -> device before and device -> host after, inside the
-timed region), so both numbers sample the same SIMP iterations.
+timed region), so both numbers sample the same SIMP iterations. ``learned_vs_plain`` then
+compares the first 5 SIMP iterations with the learned CG start and with the plain
+previous-iterate start (the network trained in the run; ``--no-learned`` skips it).
 
 N > 1 runs under torchrun with one independent replica per GPU (the solve has no
 cross-GPU exchange): value = total iterations / max rank time. ``--impl reference`` times
@@ -190,6 +192,71 @@ def replica_rate(local_ms, steps, world, device):
     return world * steps / (t / 1e3), t
 
 
+def learned_vs_plain(w, iters=5):
+    """The metric's second half: the first `iters` SIMP iterations of the workload from the same
+    start, with the learned CG start (a U-Net trained here on GPU SIMP snapshots of seeded
+    64x32x32 cantilevers and L-brackets, then combined with the previous iterate by the Galerkin
+    step and dropped once it stops paying) against the plain previous-iterate start. Each
+    iteration is timed with CUDA events, prediction included."""
+    import torch
+    from anneal_gb300 import learned as LW
+    from anneal_gb300 import optimize as OPT
+    from anneal_gb300.fem import Grid
+
+    t0 = time.time()
+    shape = (64, 32, 32)
+    samples = []
+    for seed in range(12):
+        pw = LW.seeded_problem(seed, shape)
+        snaps, fixed, free = LW.simp_snapshots(pw, 12)
+        for esc, u, F in snaps:
+            x, mask, dims, _ = LW.node_features(shape, esc, pw.E0, pw.emin, 3.0, F, fixed, free)
+            tgt, _ = LW.node_target(shape, u, dims)
+            samples.append((x, tgt, mask, dims))
+    net = LW.UNet(base=16, levels=4, seed=0)
+    hist = LW.train(samples, net, epochs=8, lr=1e-3, log=lambda *m: None)
+    t_train = time.time() - t0
+    grid = Grid(w.shape, w.h, (0, 0, 0))
+    OPT.EMIN = w.emin
+    out = {"iterations": iters, "train": {"pairs": len(samples), "shape": list(shape), "epochs": 8,
+                                          "params": net.nparam, "loss_first": hist[0], "loss_last": hist[-1],
+                                          "seconds": t_train}}
+    for arm in ("plain", "learned"):
+        ws = None
+        if arm == "learned":  # its buffers allocated by one untimed prediction
+            ws = LW.WarmStart(net, w.shape, w.E0, w.emin, 3.0)
+            m8 = torch.zeros(w.ndof, dtype=torch.uint8, device="cuda")
+            ws.predict(torch.full((w.nelem,), w.vf ** 3, device="cuda"),
+                       torch.zeros(w.ndof, dtype=torch.float64, device="cuda"), m8, m8)
+            torch.cuda.synchronize()
+        run = OPT.SimpRunner(grid, w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, w.E0, w.nu, w.vf,
+                             iters=10 ** 6, r_mm=w.r_vox, p_final=3.0, move=0.2, x0=np.full(w.nelem, w.vf),
+                             beta_max=0.0, rtol=RTOL, log=lambda *a: None, warm_start=ws)
+        ms, cg, used = [], [], []
+        for _ in range(iters):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            active = run.warm_start is not None
+            e0.record()
+            rec = run.step()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            cg.append(rec["cgIters"][0])
+            used.append(active)
+        out[arm] = {"ms_per_iteration": ms, "cg_iters": cg, "value": iters / (sum(ms) / 1e3), "unit": UNIT}
+        if arm == "learned":
+            out[arm]["network_used"] = used
+            out[arm]["initial_error_gain"] = [round(g, 6) for g in run.ws_gain]
+        run.close()
+        del ws
+        torch.cuda.empty_cache()
+    out["time_ratio_plain_over_learned"] = sum(out["plain"]["ms_per_iteration"]) / sum(
+        out["learned"]["ms_per_iteration"])
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -291,12 +358,15 @@ def run_gpu(args):
                 "ku_engine": "tensor cores (tcgen05, 3xTF32)" if os.environ.get("ANL_TC", "0") not in ("", "0")
                 else "SIMT (modal FP32)",
                 "clocks": clk.summary()}
+    run.close()
+    if rank == 0:
+        if world == 1 and not args.no_learned:
+            line["learned_vs_plain"] = learned_vs_plain(w)
         if world == 1 and not args.no_cpu_baseline:
             t, cg, threads, desc = cpu_sample(w)
             line["cpu_baseline"] = {"value": 1.0 / t, "unit": UNIT, "cores": threads, "kind": "port",
                                     "sample": desc, "cg_iters": cg}
         print(json.dumps(line), flush=True)
-    run.close()
     if world > 1:
         dist.destroy_process_group()
     return 0
@@ -309,6 +379,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-start comparison (training takes about 15 s)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
