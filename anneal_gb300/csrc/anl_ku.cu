@@ -514,10 +514,11 @@ int launch_ku(int mode, const KuArgs<T>& args, const KeModal<T>& km, cudaStream_
         case KU_CHEB0: resident = ku_resident<T, KU_CHEB0>(); break;
         default: return ANL_ERR_BADARG;
     }
-    // one wave of CTAs (shared by the batch's right-hand sides). A segment costs one extra
-    // element layer, but a plane step is a ~1 us latency chain, so small (coarse-level) grids
-    // spread over many short segments.
-    const int per_rhs = std::max(1, resident / std::max(1, a.nrhs));
+    // one wave of CTAs per right-hand side. A segment costs one extra element layer, but a
+    // plane step is a ~1 us latency chain, so small (coarse-level) grids spread over many short
+    // segments. Every slot of a batch gets the partition a single solve gets, so its sums (the
+    // p.Kp reduction follows the CTAs) and its iterates are those of its own solve.
+    const int per_rhs = std::max(1, resident);
     a.kz = (int)std::max<int64_t>(2, (total + per_rhs - 1) / per_rhs);
     const int blocks = (int)((total + a.kz - 1) / a.kz);
     dim3 block(32, KmCfg<T>::NW);

@@ -297,6 +297,27 @@ def test_six_case_bracket_160_fp32_batch_matches_oracle(golden):
     assert np.abs(x.reshape(-1, nx).sum(axis=1) - s["row_sums"]).max() < 1e-3 * nx
 
 
+def test_fp32_batch_is_the_one_by_one_solve_on_a_larger_grid():
+    """At 128x64x64 the finest K u grid no longer fits one wave per right-hand side: each slot of
+    a batch still gets the CTA partition of a single solve (its p.Kp sums follow the CTAs), so the
+    batch stays bit-identical to one solve per case."""
+    import torch
+    w = P.six_case_bracket(scale=2.0 / 3.0)
+    fem = G.FEM(_grid(w.shape), w.active, w.fixed, 0.3, precision="fp32")
+    rho = P.random_density(w.shape, 12, active=w.active)
+    E = torch.as_tensor((1e-9 + rho ** 3) * w.active, dtype=torch.float32, device="cuda")
+    mask = fem._mask_t.double()
+    keys = list(w.loads)[::2][:2]
+    F = torch.stack([torch.as_tensor(w.loads[k], device="cuda") * mask for k in keys])
+    X = torch.zeros_like(F)
+    its = fem.solve_device(E, F, X, rtol=1e-6)
+    for i in range(2):
+        Xi = torch.zeros_like(F[i:i + 1])
+        it = fem.solve_device(E, F[i:i + 1].clone(), Xi, rtol=1e-6)
+        assert it[0] == its[i] and torch.equal(Xi[0], X[i]), i
+    fem.close()
+
+
 @pytest.mark.parametrize("precision,rtol", [("auto", 1e-8), ("fp32", 1e-6)])
 def test_six_case_simp_matches_oracle(oracle, precision, rtol):
     """Six load cases (+-x, +-y, +-z: each negative case folded onto its positive one, the
