@@ -53,7 +53,7 @@ struct KuArgs {
     int c1_zero = 0;                 // CHEB: first step of a sweep (c1 = 0, d is not read)
     int dv_keep = 1;                 // CHEB, CHEB0: 0 on the last step of a sweep (d is not stored)
     const double* cheb0 = nullptr;   // CHEB0: {c1_0, c2_0} of the step from x = 0
-    const float* diag = nullptr;     // CHEB0: inverse diagonal of K per node (0 where unused)
+    const float* diag = nullptr;     // CHEB, CHEB0: inverse diagonal of K per node (0 where unused)
     T kdiag = T(0);                  // diagonal entry of Ke(1) (all 24 are equal)
     double* partials = nullptr;      // APPLY_DOT reduction scratch
     unsigned* counter = nullptr;

@@ -94,13 +94,14 @@ struct KuCarry {
     V3<T> dyb[2];  // Dy of columns ie, ie + 1
     V3<T> acc;     // forces of the layer below on node (ie, je)
     V3<T> braw;    // CHEB0: b at node (ie, je), as staged (before the D^-1 scaling)
-    float sprev;   // E summed over the 4 elements of the layer below around node (ie, je)
+    float dg;      // CHEB0: the inverse diagonal at node (ie, je), as staged
 };
 // epilogue inputs of the next output node, loaded one layer ahead
 template <class T>
 struct KuEpi {
     uint8_t nm;
     T b[3], dv[3];
+    float dg;  // CHEB: the inverse diagonal of the output node (level's diag array)
 };
 
 __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, bool valid) {
@@ -122,7 +123,7 @@ template <class T, int MODE>
 struct KuSmem {
     static constexpr int NW = KmCfg<T>::NW;
     static constexpr bool CH = MODE == KU_CHEB || MODE == KU_CHEB0;
-    static constexpr int NV = CH ? 7 : 6;  // values passed to the next warp (+ E sum)
+    static constexpr int NV = 6;           // values passed to the next warp
     T u[KU_RING][NW + 1][32][3];           // staged node values (b in CHEB0)
     float E[KU_RING][NW][32];
     float D[MODE == KU_CHEB0 ? KU_RING : 1][NW + 1][32];  // CHEB0: staged inverse diagonal
@@ -229,7 +230,8 @@ struct KuTile {
         if (MODE == KU_CHEB0) iD += plane;
     }
 
-    __device__ __forceinline__ void node_pair(int slot, V3<T> (&u)[2], V3<T>* raw0 = nullptr) const {
+    __device__ __forceinline__ void node_pair(int slot, V3<T> (&u)[2], V3<T>* raw0 = nullptr,
+                                              float* d0 = nullptr) const {
         const T* p = &sm.u[slot][w][lane][0];
         constexpr int ROW = 32 * 3;
         u[0].xy.x = p[0];
@@ -240,6 +242,7 @@ struct KuTile {
         u[1].z = p[ROW + 2];
         if (MODE == KU_CHEB0) {  // x1 = c2_0 b / diag (b is zero on non-free DOFs)
             if (raw0) *raw0 = u[0];
+            if (d0) *d0 = sm.D[slot][w][lane];
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 u[r] = (c2_0 * T(sm.D[slot][w + r][lane])) * u[r];
@@ -257,6 +260,7 @@ struct KuTile {
                 for (int c = 0; c < 3; ++c) e.b[c] = ldg_t(a.b + 3 * n + c);
             }
             if (MODE == KU_CHEB) {
+                e.dg = __ldg(a.diag + n);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) e.dv[c] = a.c1_zero ? T(0) : a.dv[3 * n + c];
             }
@@ -265,14 +269,13 @@ struct KuTile {
 
     // carry of the node plane staged in `slot` (edge differences only, no forces yet)
     __device__ __forceinline__ void start(int slot, KuCarry<T>& c) const {
-        node_pair(slot, c.ub, &c.braw);
+        node_pair(slot, c.ub, &c.braw, &c.dg);
         const V3<T> nb0 = shfl_down3(c.ub[0]), nb1 = shfl_down3(c.ub[1]);
         c.dxb[0] = nb0 - c.ub[0];
         c.dxb[1] = nb1 - c.ub[1];
         c.dyb[0] = c.ub[1] - c.ub[0];
         c.dyb[1] = nb1 - nb0;
         c.acc = v3zero<T>();
-        c.sprev = 0.f;
     }
 
     // Element layer kk (between node planes kk and kk + 1), staged in ring slot kk % KU_RING;
@@ -285,7 +288,7 @@ struct KuTile {
         issue_next(kend);
         epi_load(n + plane, owner && kk + 1 < kend, epn);
         V3<T> cu[2];
-        node_pair(slot, cu, &o.braw);
+        node_pair(slot, cu, &o.braw, &o.dg);
         const float Ee = sm.E[slot][w][lane];
         // edge differences of the upper plane
         const V3<T> un0 = shfl_down3(cu[0]), un1 = shfl_down3(cu[1]);
@@ -313,8 +316,6 @@ struct KuTile {
         for (int py = 0; py < 2; ++py)
 #pragma unroll
             for (int pz = 0; pz < 2; ++pz) f[0][py][pz] = f[0][py][pz] + shfl_up3(f[1][py][pz]);
-        float ex = 0.f;
-        if (Smem::CH) ex = Ee + __shfl_up_sync(FULL, Ee, 1);
         // y: corners py = 1 of warp w - 1 are corners py = 0 of warp w
         T* xo = &sm.x[par][w + 1][0][lane];
 #pragma unroll
@@ -323,7 +324,6 @@ struct KuTile {
             xo[(3 * pz + 1) * 32] = f[0][1][pz].xy.y;
             xo[(3 * pz + 2) * 32] = f[0][1][pz].z;
         }
-        if (Smem::CH) xo[6 * 32] = T(ex);
         cp_async_wait<KU_DEPTH - 1>();  // this thread's copies of layer kk + 1 have landed
         __syncthreads();                // ... everyone's, and the y hand-over is visible
         const T* xi = &sm.x[par][w][0][lane];
@@ -335,9 +335,7 @@ struct KuTile {
             r.z = xi[(3 * pz + 2) * 32];
             f[0][0][pz] = f[0][0][pz] + r;
         }
-        if (Smem::CH) ex += (float)xi[6 * 32];
         o.acc = f[0][0][1];
-        o.sprev = ex;
         if (emit && owner) {
             const V3<T> yv = in.acc + f[0][0][0];
             const T y[3] = {yv.xy.x, yv.xy.y, yv.z};
@@ -369,8 +367,9 @@ struct KuTile {
                     for (int c = 0; c < 3; ++c) yp[c] = (nm >> c) & 1 ? b[c] - y[c] : T(0);
                 }
             } else if (Smem::CH) {
-                const float esum = in.sprev + ex;
-                const T inv = esum > 0.f ? T(1) / (a.kdiag * T(esum)) : T(0);
+                // the level's inverse diagonal (0 on nodes without elements): staged with the
+                // plane in CHEB0, loaded with the epilogue inputs in CHEB
+                const T inv = T(MODE == KU_CHEB0 ? in.dg : ep.dg);
                 const T c1 = a.cheb ? T(a.cheb[0]) : a.c1, c2 = a.cheb ? T(a.cheb[1]) : a.c2;
                 T* dp = a.dv + 3 * n;
                 T* xp = a.xout + 3 * n;

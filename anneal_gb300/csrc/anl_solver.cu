@@ -949,6 +949,7 @@ static KuArgs<T> ku_args(anl_ctx* c, const Level& L) {
     a.d = L.d;
     a.E = L.E;
     a.nmask = L.nmask;
+    a.diag = L.diag;  // the Chebyshev passes' inverse diagonal
     a.kdiag = T(c->kdiag);
     a.partials = c->partials;
     a.counter = c->counter;
