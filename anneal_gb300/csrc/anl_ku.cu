@@ -147,6 +147,7 @@ struct KuTile {
     uint32_t s_D, s_DN;       // CHEB0: the inverse diagonal's ring entries
     const T* src_base;        // staged node field: u, or b in CHEB0
     T c2_0 = T(0);            // CHEB0: x1 = c2_0 D^-1 b
+    T c1s = T(0), c2s = T(0); // CHEB, CHEB0: the step's coefficients (read and converted once)
     const float* iD = nullptr;
     // segment geometry
     bool r0in, rNin, ein, owner;
@@ -171,6 +172,10 @@ struct KuTile {
         s_DN = (uint32_t)__cvta_generic_to_shared(&sm.D[0][NW][lane]);
         src_base = MODE == KU_CHEB0 ? a.b : a.u;
         if (MODE == KU_CHEB0) c2_0 = T(a.cheb0[1]);
+        if (MODE == KU_CHEB || MODE == KU_CHEB0) {
+            c1s = a.cheb ? T(a.cheb[0]) : a.c1;
+            c2s = a.cheb ? T(a.cheb[1]) : a.c2;
+        }
     }
 
     __device__ void set_column(int bx, int by, int k0) {
@@ -370,7 +375,7 @@ struct KuTile {
                 // the level's inverse diagonal (0 on nodes without elements): staged with the
                 // plane in CHEB0, loaded with the epilogue inputs in CHEB
                 const T inv = T(MODE == KU_CHEB0 ? in.dg : ep.dg);
-                const T c1 = a.cheb ? T(a.cheb[0]) : a.c1, c2 = a.cheb ? T(a.cheb[1]) : a.c2;
+                const T c1 = c1s, c2 = c2s;
                 T* dp = a.dv + 3 * n;
                 T* xp = a.xout + 3 * n;
 #pragma unroll
