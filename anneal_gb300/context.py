@@ -134,7 +134,8 @@ class Context:
 
     def profile_pass(self, pass_id, reps):
         """Mean milliseconds per launch of a finest-level solve pass (0 K u, 1 K u with u.Ku,
-        2 residual, 3 Chebyshev step, 4 fused first two Chebyshev steps); after a solve."""
+        2 residual, 3 last Chebyshev step of a sweep, 4 fused first two Chebyshev steps, 5 first step
+        of the post-smoothing sweep); after a solve."""
         ms = ctypes.c_double(0.0)
         N.check(self.lib.anl_profile_pass(self._h, int(pass_id), int(reps), ctypes.byref(ms), _stream()),
                 "anl_profile_pass")

@@ -682,8 +682,8 @@ __global__ void k_oc_decide(OcState* st, const double* vols) {
     if (!st->stop) oc_make_bank(st, threadIdx.x);
 }
 
-constexpr int OCB_T = 512;  // threads of a bank pass: two CTAs per SM, each thread ~27 elements at 12.8M DOF
-__global__ void __launch_bounds__(OCB_T, 2) k_oc_vol_bank(int64_t ne, const float4* __restrict__ el,
+constexpr int OCB_T = 512;  // threads of a bank pass: one CTA per SM, each thread ~54 elements at 12.8M DOF
+__global__ void __launch_bounds__(OCB_T, 1) k_oc_vol_bank(int64_t ne, const float4* __restrict__ el,
                                                     const float2* __restrict__ gw, const OcState* st,
                                                     double* partials, unsigned* counter, double* out) {
     if (st->stop) return;  // the same for every block
@@ -696,19 +696,27 @@ __global__ void __launch_bounds__(OCB_T, 2) k_oc_vol_bank(int64_t ne, const floa
         rl[j] = oc_rl(bank.lam[j]);
     }
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += 2 * stride) {
-        // two elements per iteration, their loads issued before either is used
-        const bool two = e + stride < ne;
-        const float4 q0 = el[e];
-        const float2 t0 = gw[e];
-        const float4 q1 = two ? el[e + stride] : make_float4(0.f, 1.f, 0.f, 0.f);
-        const float2 t1 = two ? gw[e + stride] : make_float2(0.f, 0.f);
+    constexpr int U = 4;  // elements per trip, their loads issued before any is used
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += U * stride) {
+        float4 q[U];
+        float2 t[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool in = e + u * stride < ne;
+            q[u] = in ? el[e + u * stride] : make_float4(0.f, 1.f, 0.f, 0.f);
+            t[u] = in ? gw[e + u * stride] : make_float2(0.f, 0.f);
+        }
 #pragma unroll
         for (int j = 0; j < OC_BANK; ++j) {
             if (j < bank.n) {  // oc_xn with the elements' lambda-free parts
-                const float v0 = q0.y * bank.lam[j] > 1e-30f ? fminf(fmaxf(q0.x * rl[j], q0.z), q0.w) : t0.x;
-                const float v1 = q1.y * bank.lam[j] > 1e-30f ? fminf(fmaxf(q1.x * rl[j], q1.z), q1.w) : t1.x;
-                acc[j] = fmaf(t1.y, v1, fmaf(t0.y, v0, acc[j]));
+                float a = acc[j];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const float v = q[u].y * bank.lam[j] > 1e-30f ? fminf(fmaxf(q[u].x * rl[j], q[u].z), q[u].w)
+                                                                   : t[u].x;
+                    a = fmaf(t[u].y, v, a);
+                }
+                acc[j] = a;
             }
         }
     }
@@ -778,7 +786,7 @@ int oc_update(anl_ctx* c, const float* x, const float* dcx, const float* dvx, co
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         }
-        const int bank_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(2 * sms, (ne + OCB_T - 1) / OCB_T));
+        const int bank_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(sms, (ne + OCB_T - 1) / OCB_T));
         for (int round = 0; round < 100 / OC_BANK_DEPTH + 1; ++round) {
             for (int q = 0; q < passes; ++q) {
                 k_oc_vol_bank<<<bank_blocks, OCB_T, 0, s>>>(ne, c->oc_el, c->oc_gw, st, c->partials, c->counter,

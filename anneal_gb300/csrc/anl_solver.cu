@@ -1808,9 +1808,14 @@ int solver_profile_pass(anl_ctx* c, int pass, int reps, double* ms, cudaStream_t
             a.u = (const float*)L.x; a.b = (const float*)L.b; a.dv = (float*)L.dv; a.xout = (float*)L.xt;
             a.cheb = cf + 2; a.c1_zero = 0; a.dv_keep = 0; mode = KU_CHEB;  // the last step of a sweep
             break;
+        case 5:
+            a.u = (const float*)L.x; a.b = (const float*)L.b; a.dv = (float*)L.dv; a.xout = (float*)L.xt;
+            a.cheb = cf; a.c1_zero = 1; a.dv_keep = 1; mode = KU_CHEB;  // the first step of a sweep from x != 0
+            break;
         case 4:
             a.b = (const float*)L.b; a.diag = L.diag; a.dv = (float*)L.dv; a.xout = (float*)L.x;
-            a.cheb0 = cf; a.cheb = cf + 2; a.dv_keep = 1; mode = KU_CHEB0;
+            // as the V-cycle runs it: the direction is kept only for a sweep of more than 2 steps
+            a.cheb0 = cf; a.cheb = cf + 2; a.dv_keep = c->mg_degree > 2; mode = KU_CHEB0;
             break;
         default: set_error("profile pass: unknown pass %d", pass); return ANL_ERR_BADARG;
     }

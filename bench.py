@@ -38,12 +38,14 @@ RTOL = 1e-6
 
 # finest-level solve passes: (profile id, name, launches per CG iteration, algorithmic bytes(N_n, N_e))
 # K u reads u and E and writes y; the residual also reads b; the last Chebyshev step of a sweep
-# reads x, b, the direction and the inverse diagonal and writes x; the fused first two steps read
-# b and the inverse diagonal and write x and d
+# reads x, b, the direction and the inverse diagonal and writes x (the first step of the
+# post-smoothing reads x, b and the inverse diagonal and writes x and the direction); the fused
+# first two steps read b and the inverse diagonal and write x
 PASSES = [
     (1, "K u with u.Ku (CG q = K p)", 1, lambda nn, ne: 24 * nn + 4 * ne),
     (2, "residual b - K x", 1, lambda nn, ne: 36 * nn + 4 * ne),
-    (3, "Chebyshev step", 2, lambda nn, ne: 52 * nn + 4 * ne),
+    (3, "last Chebyshev step of a sweep", 1, lambda nn, ne: 52 * nn + 4 * ne),
+    (5, "first Chebyshev step after the prolongation", 1, lambda nn, ne: 52 * nn + 4 * ne),
     (4, "first two Chebyshev steps", 1, lambda nn, ne: 40 * nn + 4 * ne),
     (0, "K u", 0, lambda nn, ne: 24 * nn + 4 * ne),
 ]

@@ -315,8 +315,9 @@ int anl_profile_apply(anl_ctx* ctx, const void* u, void* y, int reps, double* ms
 /* Benchmark hook (no counterpart in the reference): times one finest-level pass of the solve,
    `reps` launches between two CUDA events on `stream`, on the context's own work vectors:
    pass 0 K u, 1 K u with the u.Ku reduction (the CG's q = K p), 2 the residual b - K x, 3 the
-   last Chebyshev step of a smoothing sweep, 4 the first two Chebyshev steps fused. The mean milliseconds per
-   launch go to *ms_h. FP32 contexts, after at least one anl_solve; it overwrites the V-cycle
+   last Chebyshev step of a smoothing sweep, 4 the first two Chebyshev steps fused, 5 the first step of a
+   sweep that starts from a nonzero iterate (the post-smoothing after the prolongation). The mean
+   milliseconds per launch go to *ms_h. FP32 contexts, after at least one anl_solve; it overwrites the V-cycle
    scratch (the next solve starts afresh), so do not call it during a stream capture. */
 int anl_profile_pass(anl_ctx* ctx, int pass, int reps, double* ms_h, anl_stream_t stream);
 
