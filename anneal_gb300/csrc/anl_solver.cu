@@ -287,8 +287,10 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
 
 // x_f += P x_c on free fine DOFs (trilinear interpolation of the coarse correction). One
 // thread per coarse node (I, J, K) updates the up to 8 fine nodes (2I + a, 2J + b, 2K + g),
-// a, b, g in {0, 1}, from the up to 8 coarse nodes (I + a', J + b', K + g'): every load of a
-// thread is independent of the others, so the loads of a warp overlap.
+// a, b, g in {0, 1}, from the up to 8 coarse nodes (I + a', J + b', K + g'). Every load of a
+// thread (coarse values, fine masks and fine values) is issued before the first store and
+// none depends on another, so one memory latency covers all of them (with the fine loads
+// behind a test of their mask, each fine node cost two latencies in turn: 38 us at 12.8M DOF).
 template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
                                                                 const uint8_t* __restrict__ nmf, T* __restrict__ xf,
@@ -315,23 +317,34 @@ __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, 
 #pragma unroll
                 for (int e = 0; e < 3; ++e) v[g][bb][a][e] = in ? __ldg(q + e) : T(0);
             }
+    // fine node values and masks (mask 0 beyond the fine grid: nothing stored there)
+    T xv[2][2][2][3];
+    uint8_t mv[2][2][2];
 #pragma unroll
-    for (int g = 0; g < 2; ++g) {
-        const int k = 2 * K + g;
-        if (k > f.nz) continue;
+    for (int g = 0; g < 2; ++g)
 #pragma unroll
-        for (int bb = 0; bb < 2; ++bb) {
-            const int j = 2 * J + bb;
-            if (j > f.ny) continue;
+        for (int bb = 0; bb < 2; ++bb)
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
-                const int i = 2 * I + a;
-                if (i > f.nx) continue;
-                const int64_t n = (int64_t)k * fxy + (int64_t)j * fx + i;
-                const uint8_t m = nmf[n];
+                const int i = 2 * I + a, j = 2 * J + bb, k = 2 * K + g;
+                const bool in = i <= f.nx && j <= f.ny && k <= f.nz;
+                const int64_t n = in ? (int64_t)k * fxy + (int64_t)j * fx + i : 0;
+                mv[g][bb][a] = in ? __ldg(nmf + n) : uint8_t(0);
+#pragma unroll
+                for (int e = 0; e < 3; ++e) xv[g][bb][a][e] = in ? xf[3 * n + e] : T(0);
+            }
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+        for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const uint8_t m = mv[g][bb][a];
                 if (!(m & 7)) continue;
+                const int64_t n = (int64_t)(2 * K + g) * fxy + (int64_t)(2 * J + bb) * fx + (2 * I + a);
                 // fine node (i, j, k): the mean of the coarse nodes it lies between
-                T acc[3];
+                const T w = (a ? T(0.5) : T(1)) * (bb ? T(0.5) : T(1)) * (g ? T(0.5) : T(1));
+                T* o = xf + 3 * n;
 #pragma unroll
                 for (int e = 0; e < 3; ++e) {
                     T t = v[0][0][0][e];
@@ -343,16 +356,9 @@ __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, 
                         if (bb) u += v[1][1][0][e] + (a ? v[1][1][1][e] : T(0));
                         t += u;
                     }
-                    acc[e] = t;
+                    if ((m >> e) & 1) o[e] = xv[g][bb][a][e] + w * t;
                 }
-                const T w = (a ? T(0.5) : T(1)) * (bb ? T(0.5) : T(1)) * (g ? T(0.5) : T(1));
-                T* o = xf + 3 * n;
-                if (m & 1) o[0] += w * acc[0];
-                if (m & 2) o[1] += w * acc[1];
-                if (m & 4) o[2] += w * acc[2];
             }
-        }
-    }
 }
 
 // x = d = c2 D^-1 b  (first Chebyshev step from x = 0)
