@@ -46,7 +46,7 @@ PASSES = [
     (2, "residual b - K x", 1, lambda nn, ne: 36 * nn + 4 * ne),
     (3, "last Chebyshev step of a sweep", 1, lambda nn, ne: 52 * nn + 4 * ne),
     (5, "first Chebyshev step after the prolongation", 1, lambda nn, ne: 52 * nn + 4 * ne),
-    (4, "first two Chebyshev steps", 1, lambda nn, ne: 40 * nn + 4 * ne),
+    (4, "first two Chebyshev steps", 1, lambda nn, ne: 28 * nn + 4 * ne),
     (0, "K u", 0, lambda nn, ne: 24 * nn + 4 * ne),
 ]
 
