@@ -168,6 +168,35 @@ def _lbracket_run(golden, name, scale):
     return s, c, vol, x
 
 
+def test_history_start_saves_cg_iterations_at_the_same_results():
+    """The opt-in CG start from the last two solutions (their Galerkin combination) against the
+    reference's previous-solution start (optimize.py:122) on the FP32 path: fewer CG iterations
+    over SIMP iterations 3-10, the same compliances and design within the parity bars."""
+    import torch
+    w = P.lbracket(scale=1 / 3, vf=0.25, r_vox=2.0, emin=1e-9)
+    old = O.EMIN
+    O.EMIN = 1e-9
+    out = {}
+    try:
+        for start in ("previous", "history"):
+            run = O.SimpRunner(_grid(w.shape), w.fill, w.active, w.frozen, w.fixed, w.loads, w.weights, w.E0,
+                               w.nu, w.vf, iters=10, r_mm=w.r_vox, p_final=3.0, move=0.2,
+                               x0=np.full(w.nelem, w.vf), beta_max=0.0, rtol=1e-6, log=lambda *a: None,
+                               precision="fp32", cg_start=start)
+            hist = [run.step() for _ in range(10)]
+            out[start] = (np.array([h["cgIters"][0] for h in hist]), np.array([h["compliance"][0] for h in hist]),
+                          run.xphys_t.cpu().numpy().astype(float))
+            run.close()
+            torch.cuda.empty_cache()
+    finally:
+        O.EMIN = old
+    (cg_p, c_p, x_p), (cg_h, c_h, x_h) = out["previous"], out["history"]
+    assert np.array_equal(cg_p[:2], cg_h[:2])  # the same start until two solutions exist
+    assert cg_h[2:].sum() < cg_p[2:].sum(), (cg_h, cg_p)
+    assert np.abs(c_h / c_p - 1).max() < 1e-5
+    assert np.abs(x_h - x_p).max() < 1e-3
+
+
 def test_config2_lbracket_192_fp32_30_iterations_match_oracle(golden):
     """Config 2: the 192x96x96 L-bracket (5.45M DOF), 30 iterations at CG rtol 1e-6: compliance
     of every iteration within 1e-5 and the final density within 1e-3 (L-inf) of the oracle."""
