@@ -126,6 +126,8 @@ class SimpRunner:
         self.F_t = to_dev(F_host, torch.float64)
         self.U_t = torch.zeros_like(self.F_t)
         self._U_prev = None     # the solutions of the solve before the last (cg_start "history")
+        # a list makes step() record a pair of CUDA events around each solve into it
+        self.solve_events = None
         self.beta = beta_max / 2 if self.warm else 0.0
         self.beta_step = max(5, int(0.12 * iters))
         self.beta_since = 0
@@ -169,7 +171,13 @@ class SimpRunner:
         elif self.cg_start == "history" and it > 1:
             self._history_start()
         t_solve = time.perf_counter()
+        if self.solve_events is not None:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record()
         fem.solve_device(self.escale_t, self.F_t, self.U_t, rtol=self.rtol, maxiter=self.maxiter, rebuild=rebuild)
+        if self.solve_events is not None:
+            ev[1].record()
+            self.solve_events.append(ev)
         if ws is not None:
             self._assess_learned_start(ws, time.perf_counter() - t_solve)
         if rebuild:

@@ -36,6 +36,11 @@ SCALE = 4.0 / 3.0          # 256 x 128 x 128 voxels
 RTOL = 1e-6
 
 
+# FP32 operations per element of K u: the dense 24 x 24 product, and the modal form (forward
+# transform from edge differences, the sparse modal stiffness times E, the inverse transform)
+KU_DENSE_FLOPS = 2 * 24 * 24
+KU_MODAL_FLOPS = 210
+
 # finest-level solve passes: (profile id, name, launches per CG iteration, algorithmic bytes(N_n, N_e))
 # K u reads u and E and writes y; the residual also reads b; the last Chebyshev step of a sweep
 # reads x, b, the direction and the inverse diagonal and writes x (the first step of the
@@ -306,6 +311,7 @@ def run_gpu(args):
     total_ms = e2e_ms = 0.0
     launches = 0
     cg_dev, cg_e2e = [], []
+    solve_ev = []
     with ClockSampler(local) as clk:
         for s in range(2 * args.steps):
             device = s % 2 == 0
@@ -315,6 +321,7 @@ def run_gpu(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             n0, c0 = lib.anl_launch_count(), len(run.fem.cg_iters)
+            run.solve_events = solve_ev if device else None
             e0.record(stream)
             if device:
                 run.step()
@@ -330,6 +337,8 @@ def run_gpu(args):
                 e2e_ms += e0.elapsed_time(e1)
                 cg_e2e += run.fem.cg_iters[c0:]
     barrier()
+    run.solve_events = None
+    solve_ms = sum(a.elapsed_time(b) for a, b in solve_ev)
     cg_counts = cg_dev
     value, t_max = replica_rate(total_ms, args.steps, world, "cuda")
     e2e, e2e_ms = replica_rate(e2e_ms, args.steps, world, "cuda")
@@ -355,6 +364,25 @@ def run_gpu(args):
                        "algorithmic_bytes": b, "GBps": b / (ms * 1e-3) / 1e9,
                        "frac": b / (ms * 1e-3) / 1e9 / peak})
     dom = max(passes, key=lambda q: q["ms_per_launch"] * q["launches_per_cg_iteration"])
+    # K u in DOF/s and as a FLOP fraction: the dense-equivalent 1,152 flops per element (the
+    # 24 x 24 Ke times u_e) and the ~210 FP32 operations the modal form executes, against the
+    # FP32 CUDA-core peak (SMs x 128 lanes x 2 flops x the sampled SM clock)
+    clocks = clk.summary()
+    ku_ms = next(q["ms_per_launch"] for q in passes if q["pass"] == "K u")
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sms * 128 * 2 * ((clocks or {}).get("sm_mhz") or 2070.0) * 1e6 / 1e12
+    ku_line = {"dofs_per_s": 3 * nn / (ku_ms * 1e-3), "ms_per_launch": ku_ms,
+               "tflops_dense_equivalent": KU_DENSE_FLOPS * ne / (ku_ms * 1e-3) / 1e12,
+               "tflops_executed": KU_MODAL_FLOPS * ne / (ku_ms * 1e-3) / 1e12,
+               "fp32_peak_tflops": fp32_peak,
+               "executed_frac": KU_MODAL_FLOPS * ne / (ku_ms * 1e-3) / 1e12 / fp32_peak}
+    # PCG solves of the device-timed steps (CUDA events around each solve: set-up of the
+    # hierarchy and the coarsest factor, the CG iterations, the accurate residuals)
+    nsolve = len(solve_ev)
+    pcg_line = {"solves_per_s": nsolve / (solve_ms / 1e3) if solve_ms > 0 else None,
+                "ms_per_solve": solve_ms / nsolve if nsolve else None,
+                "ms_per_cg_iteration": solve_ms / sum(cg_dev) if cg_dev else None,
+                "share_of_step": solve_ms / total_ms if total_ms > 0 else None}
     traffic = None  # DRAM bytes come from an ncu capture (profiles/), never from this timed run
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -373,9 +401,11 @@ def run_gpu(args):
                              "ms_per_launch": dom["ms_per_launch"],
                              "timing": "one launch after a 512 MB L2 flush, median of 20"},
                 "roofline_passes": passes,
+                "ku": ku_line,
+                "pcg": pcg_line,
                 "ku_engine": "tensor cores (tcgen05, 3xTF32)" if os.environ.get("ANL_TC", "0") not in ("", "0")
                 else "SIMT (modal FP32)",
-                "clocks": clk.summary()}
+                "clocks": clocks}
     run.close()
     if rank == 0:
         if world == 1 and not args.no_learned:
