@@ -7,7 +7,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libanneal_gb300.so")
+# ANL_DEBUG_LIB=1 loads the bounds-checked debug build (python -m anneal_gb300.build --debug)
+DEBUG_LIB = os.environ.get("ANL_DEBUG_LIB", "0") not in ("", "0")
+LIB_PATH = os.path.join(HERE, "_lib_debug" if DEBUG_LIB else "_lib", "libanneal_gb300.so")
 
 ANL_OK = 0
 ANL_ERR_MAXITER = 1
@@ -41,7 +43,7 @@ EXPORTS = [
     "anl_mc_table", "anl_nn_conv3d", "anl_nn_conv3d_bwd_data", "anl_nn_conv3d_bwd_weight", "anl_nn_gelu_bwd",
     "anl_nn_pool2", "anl_nn_up2", "anl_nn_mse", "anl_nn_adam", "anl_element_stress",
     "anl_vox_create", "anl_vox_destroy", "anl_voxel_fill", "anl_output_field", "anl_choose_level",
-    "anl_label_above", "anl_edt", "anl_profile_pass", "anl_solve_status",
+    "anl_label_above", "anl_edt", "anl_profile_pass", "anl_solve_status", "anl_debug_oob",
 ]
 
 
@@ -83,6 +85,7 @@ _SIGS = {
     "anl_profile_apply": (I, [P, P, P, I, ctypes.POINTER(D), P]),
     "anl_profile_pass": (I, [P, I, I, ctypes.POINTER(D), P]),
     "anl_launch_count": (I64, []),
+    "anl_debug_oob": (I, [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     "anl_mg_info": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)]),
     "anl_dot_static": (I, [P, P, I64, P, P]),
     "anl_mc_create": (I, [ctypes.POINTER(P)]),
@@ -122,7 +125,7 @@ def load():
         return _lib
     if not os.path.isfile(LIB_PATH):
         raise ImportError(f"{LIB_PATH} is missing: build the CUDA library first "
-                          f"(python -m anneal_gb300.build)")
+                          f"(python -m anneal_gb300.build{' --debug' if DEBUG_LIB else ''})")
     lib = ctypes.CDLL(LIB_PATH)
     for name, (res, args) in _SIGS.items():
         fn = getattr(lib, name)

@@ -493,6 +493,23 @@ const char* anl_last_error(void) { return anl::g_err; }
 
 int64_t anl_launch_count(void) { return (int64_t)anl::g_launches.load(); }
 
+int anl_debug_oob(long long* count_h, long long* first_h) {
+    NEED(count_h && first_h, "anl_debug_oob: null argument");
+    first_h[0] = first_h[1] = first_h[2] = 0;
+#if ANL_DEBUG
+    unsigned long long n = 0;
+    ANL_TRY(anl::debug_take_ku(&n, first_h));
+    ANL_TRY(anl::debug_take_kbox(&n, first_h));
+    ANL_TRY(anl::debug_take_solver(&n, first_h));
+    ANL_TRY(anl::debug_take_design(&n, first_h));
+    ANL_TRY(anl::debug_take_vtail(&n, first_h));
+    *count_h = (long long)n;
+#else
+    *count_h = -1;
+#endif
+    return ANL_OK;
+}
+
 int anl_ctx_create(anl_ctx** out, int nx, int ny, int nz, double h, double nu, int flags) {
     anl::g_err[0] = 0;
     std::lock_guard<std::recursive_mutex> lock(anl::device_sync_mutex());

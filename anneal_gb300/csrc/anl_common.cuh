@@ -49,6 +49,50 @@ namespace anl {
 
 void set_error(const char* fmt, ...);
 
+// ------------------------------------------------------------------ debug bounds checks
+//
+// ANL_IN_RANGE(i, n) is `true` in the normal build. In the debug build (-DANL_DEBUG=1,
+// `python -m anneal_gb300.build --debug`, loaded with ANL_DEBUG_LIB=1) it tests 0 <= i < n for
+// a global-memory index before the access; a miss is counted in this translation unit's
+// device record (the first miss keeps its index, extent and source line) and the caller skips
+// the access, so a bad index is reported instead of touching memory out of range.
+// anl_debug_oob collects the records of every unit. Without relocatable device code each
+// unit has its own record: ANL_DEBUG_UNIT(name) defines the unit's reader.
+#if ANL_DEBUG
+struct OobRecord {
+    unsigned long long count;
+    long long index, extent, line;
+};
+static __device__ OobRecord g_oob;
+__device__ __forceinline__ bool debug_in_range(long long i, long long n, int line) {
+    if (i >= 0 && i < n) return true;
+    if (atomicAdd(&g_oob.count, 1ull) == 0ull) {
+        g_oob.index = i;
+        g_oob.extent = n;
+        g_oob.line = line;
+    }
+    return false;
+}
+#define ANL_IN_RANGE(i, n) ::anl::debug_in_range((long long)(i), (long long)(n), __LINE__)
+// reads and clears this unit's record (host)
+#define ANL_DEBUG_UNIT(name)                                                        \
+    int debug_take_##name(unsigned long long* count, long long* first) {          \
+        OobRecord r{}, z{};                                                          \
+        ANL_CUDA(cudaMemcpyFromSymbol(&r, g_oob, sizeof(r)));                       \
+        ANL_CUDA(cudaMemcpyToSymbol(g_oob, &z, sizeof(z)));                         \
+        *count += r.count;                                                           \
+        if (r.count && first[2] == 0) {                                              \
+            first[0] = r.index;                                                      \
+            first[1] = r.extent;                                                     \
+            first[2] = r.line;                                                       \
+        }                                                                            \
+        return ANL_OK;                                                               \
+    }
+#else
+#define ANL_IN_RANGE(i, n) true
+#define ANL_DEBUG_UNIT(name)
+#endif
+
 // Held while a stream is captured into a CUDA graph and around every call that synchronises
 // the whole device (cudaFree, cudaFreeHost, context set-up): such a call from another host
 // thread would invalidate an ongoing capture, and several contexts may run in parallel

@@ -85,6 +85,7 @@ __device__ __forceinline__ float filter_input(const FilterArgs& a, int gi, int g
     const Dims& d = a.d;
     if (gi < 0 || gj < 0 || gk < 0 || gi >= d.nx || gj >= d.ny || gk >= d.nz) return 0.f;
     const int64_t e = d.elem(gi, gj, gk);
+    if (!ANL_IN_RANGE(e, d.ne())) return 0.f;
     const bool act = a.active[e] != 0;
     float v = 1.f;
     if (MODE == F_FWD || MODE == F_PHYS) v = a.in[e];
@@ -146,9 +147,10 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
     for (int k = kb; k < kend; ++k) {
         // this layer's epilogue inputs, loaded before the barrier so their latency overlaps it
         const int64_t e = in_xy ? d.elem(i, j, k) : 0;
+        const bool in_e = in_xy && ANL_IN_RANGE(e, d.ne());
         bool act = false, fzn = false;
         float hs = 1.f, ph = 0.f;
-        if (in_xy) {
+        if (in_e) {
             act = a.active[e] != 0;
             if (MODE == F_FWD || MODE == F_PHYS || MODE == F_OCVOL) hs = a.Hs[e];
             if (MODE == F_PHYS || MODE == F_OCVOL) fzn = a.frozen[e] != 0;
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(FT_N) k_filter(FilterArgs a) {
             stage(k + R);
         }
         __syncthreads();
-        if (in_xy) {
+        if (in_e) {
             float s = 0.f;
             if (RT == 1) {
 #pragma unroll
@@ -363,6 +365,7 @@ __device__ __forceinline__ float element_energy(const KeModal<float>& K, const D
                                                 int k) {
     const int64_t sx = 1, sy = d.nx + 1, sz = (int64_t)(d.nx + 1) * (d.ny + 1);
     const int64_t n0 = d.node(i, j, k);
+    if (!ANL_IN_RANGE(n0, d.nn()) || !ANL_IN_RANGE(n0 + sx + sy + sz, d.nn())) return 0.f;
     float ch[2][2][2][3], cl[2][2][2][3];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -946,5 +949,7 @@ int design_stats(anl_ctx* c, const float* xold, const float* xnew, const float* 
     for (int q = 0; q < 4; ++q) out[q] = c->red_h[q];
     return ANL_OK;
 }
+
+ANL_DEBUG_UNIT(design)
 
 }  // namespace anl

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(BT) kbox_kernel(KbArgs a, KeModal<float> km) {
     const bool owner = t < BON;
     const int ax = 1 + t % BO, ay = 1 + (t / BO) % BO, az = 1 + t / (BO * BO);
     const int gi = ox + ax, gj = oy + ay, gk = oz + az;
-    const bool emit = owner && gi < NXn && gj < NYn && gk < NZn;
+    const bool emit = owner && gi < NXn && gj < NYn && gk < NZn && ANL_IN_RANGE(d.node(gi, gj, gk), d.nn());
     const int64_t on = emit ? d.node(gi, gj, gk) : 0;
     uint8_t nm = 0;
     float inv = 0.f, bo[3] = {0.f, 0.f, 0.f}, dprev[3] = {0.f, 0.f, 0.f};
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(BT) kbox_kernel(KbArgs a, KeModal<float> km) {
         for (int q = t; q < BCN; q += BT) {
             const int I = cox + q % BC, J = coy + (q / BC) % BC, K = coz + q / (BC * BC);
             float v0 = 0.f, v1 = 0.f, v2 = 0.f;
-            if (I <= dc.nx && J <= dc.ny && K <= dc.nz) {
+            if (I <= dc.nx && J <= dc.ny && K <= dc.nz && ANL_IN_RANGE(dc.node(I, J, K), dc.nn())) {
                 const float* p = a.xc + 3 * dc.node(I, J, K);
                 v0 = p[0];
                 v1 = p[1];
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(BT) kbox_kernel(KbArgs a, KeModal<float> km) {
         const int lx = q % BN, ly = (q / BN) % BN, lz = q / (BN * BN);
         const int i = ox + lx, j = oy + ly, k = oz + lz;
         float v[3] = {0.f, 0.f, 0.f};
-        if (i >= 0 && j >= 0 && k >= 0 && i < NXn && j < NYn && k < NZn) {
+        if (i >= 0 && j >= 0 && k >= 0 && i < NXn && j < NYn && k < NZn && ANL_IN_RANGE(d.node(i, j, k), d.nn())) {
             const int64_t n = d.node(i, j, k);
             if (MODE == KB_CHEB0) {  // x1 = c2_0 D^-1 b (b is zero on non-free DOFs)
                 const float s = c20 * __ldg(a.diag + n);
@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(BT) kbox_kernel(KbArgs a, KeModal<float> km) {
     const int tx = t & (BE - 1), ty = (t / BE) & (BE - 1), tz = t / (BE * BE);
     {
         const int i = ox + tx, j = oy + ty, k = oz + tz;
-        const bool in = i >= 0 && j >= 0 && k >= 0 && i < d.nx && j < d.ny && k < d.nz;
+        const bool in = i >= 0 && j >= 0 && k >= 0 && i < d.nx && j < d.ny && k < d.nz &&
+                        ANL_IN_RANGE(d.elem(i, j, k), d.ne());
         sE[t] = in ? __ldg(a.E + d.elem(i, j, k)) : 0.f;
     }
     __syncthreads();
@@ -277,5 +278,7 @@ int launch_kbox(int mode, const KbArgs& a, const KeModal<float>& km, cudaStream_
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }
+
+ANL_DEBUG_UNIT(kbox)
 
 }  // namespace anl

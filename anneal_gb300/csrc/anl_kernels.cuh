@@ -183,5 +183,15 @@ int kutc_prepare(const double* ke);
 int launch_kutc(int mode, const KuArgs<float>& a, const KeModal<float>& km, cudaStream_t s);
 int kutc_error_flag(int* out_h);
 
+// ------------------------------------------------------------------ debug build
+
+// The out-of-range records of the checked translation units (ANL_IN_RANGE, anl_common.cuh).
+#if ANL_DEBUG
+int debug_take_ku(unsigned long long* count, long long* first);
+int debug_take_kbox(unsigned long long* count, long long* first);
+int debug_take_solver(unsigned long long* count, long long* first);
+int debug_take_design(unsigned long long* count, long long* first);
+int debug_take_vtail(unsigned long long* count, long long* first);
+#endif
 
 }  // namespace anl

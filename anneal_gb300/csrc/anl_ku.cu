@@ -200,12 +200,13 @@ struct KuTile {
             const int pk = ik + 1;
             const bool kin = pk >= 0 && pk < NZn;
             const uint32_t so = (uint32_t)(ik & (KU_RING - 1));
-            const bool q0 = kin && r0in;
+            const int64_t nq = n0 + (int64_t)pk * plane;  // this thread's staged node
+            const bool q0 = kin && r0in && ANL_IN_RANGE(nq, plane * NZn);
             const T* src = q0 ? iu : src_base;
             if (MODE == KU_CHEB0) {
                 cp_async4(s_D + so * (uint32_t)sizeof(sm.D[0]), q0 ? iD : a.diag, q0);
                 if (w == NW - 1) {
-                    const bool qn = kin && rNin;
+                    const bool qn = kin && rNin && ANL_IN_RANGE(nq + NXn, plane * NZn);
                     cp_async4(s_DN + so * (uint32_t)sizeof(sm.D[0]), qn ? iD + NXn : a.diag, qn);
                 }
             }
@@ -216,7 +217,7 @@ struct KuTile {
                 else cp_async8(d, src + (q0 ? c : 0), q0);
             }
             if (w == NW - 1) {  // node row je + 1 of the last warp
-                const bool qn = kin && rNin;
+                const bool qn = kin && rNin && ANL_IN_RANGE(nq + NXn, plane * NZn);
                 const T* srcn = qn ? iu + 3 * NXn : src_base;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -225,7 +226,7 @@ struct KuTile {
                     else cp_async8(d, srcn + (qn ? c : 0), qn);
                 }
             }
-            const bool qe = ein && ik >= 0 && ik < a.d.nz;
+            const bool qe = ein && ik >= 0 && ik < a.d.nz && ANL_IN_RANGE(e0 + (int64_t)ik * eplane, eplane * a.d.nz);
             cp_async4(s_E + so * SLOT_E, qe ? iE : a.E, qe);
         }
         cp_async_commit();
@@ -258,7 +259,7 @@ struct KuTile {
     // epilogue loads of output node n (plane kk)
     __device__ __forceinline__ void epi_load(int64_t n, bool emit, KuEpi<T>& e) const {
         e.nm = 0;
-        if (emit) {
+        if (emit && ANL_IN_RANGE(n, plane * NZn)) {
             e.nm = __ldg(a.nmask + n);
             if (MODE == KU_RESID || MODE == KU_CHEB) {  // CHEB0 has b staged already
 #pragma unroll
@@ -341,7 +342,7 @@ struct KuTile {
             f[0][0][pz] = f[0][0][pz] + r;
         }
         o.acc = f[0][0][1];
-        if (emit && owner) {
+        if (emit && owner && ANL_IN_RANGE(n, plane * NZn)) {
             const V3<T> yv = in.acc + f[0][0][0];
             const T y[3] = {yv.xy.x, yv.xy.y, yv.z};
             const T u[3] = {in.ub[0].xy.x, in.ub[0].xy.y, in.ub[0].z};
@@ -575,5 +576,7 @@ int ku_grid_blocks(const Dims& d) {
 
 template int launch_ku<float>(int, const KuArgs<float>&, const KeModal<float>&, cudaStream_t);
 template int launch_ku<double>(int, const KuArgs<double>&, const KeModal<double>&, cudaStream_t);
+
+ANL_DEBUG_UNIT(ku)
 
 }  // namespace anl

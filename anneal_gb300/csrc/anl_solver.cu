@@ -242,7 +242,10 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
         for (int qq = 0; qq < QPT; ++qq) {
             const int q = threadIdx.x + qq * TR_X;
             const int i = fi0 + q / 3;
-            v[rr][qq] = rin && q < 3 * TRF_X && i >= 0 && i <= f.nx ? __ldg(src + q) : T(0);
+            v[rr][qq] = rin && q < 3 * TRF_X && i >= 0 && i <= f.nx &&
+                                ANL_IN_RANGE((int64_t)k * fxy + (int64_t)j * fx + i, fxy * (f.nz + 1))
+                            ? __ldg(src + q)
+                            : T(0);
         }
     }
 #pragma unroll
@@ -278,6 +281,7 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
         }
     }
     const int64_t n = (int64_t)I + (int64_t)(c.nx + 1) * ((int64_t)J + (int64_t)(c.ny + 1) * K);
+    if (!ANL_IN_RANGE(n, c.nn())) return;
     const uint8_t m = nmc[n];
     T* o = bc + 3 * n;
     o[0] = (m & 1) ? acc0 : T(0);
@@ -312,8 +316,9 @@ __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, 
         for (int bb = 0; bb < 2; ++bb)
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
-                const bool in = I + a <= c.nx && J + bb <= c.ny && K + g <= c.nz;
-                const T* q = xc + 3 * ((int64_t)(K + g) * cxy + (int64_t)(J + bb) * cx + (I + a));
+                const int64_t cn = (int64_t)(K + g) * cxy + (int64_t)(J + bb) * cx + (I + a);
+                const bool in = I + a <= c.nx && J + bb <= c.ny && K + g <= c.nz && ANL_IN_RANGE(cn, cxy * (c.nz + 1));
+                const T* q = xc + 3 * cn;
 #pragma unroll
                 for (int e = 0; e < 3; ++e) v[g][bb][a][e] = in ? __ldg(q + e) : T(0);
             }
@@ -327,8 +332,9 @@ __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, 
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
                 const int i = 2 * I + a, j = 2 * J + bb, k = 2 * K + g;
-                const bool in = i <= f.nx && j <= f.ny && k <= f.nz;
-                const int64_t n = in ? (int64_t)k * fxy + (int64_t)j * fx + i : 0;
+                const int64_t nf = (int64_t)k * fxy + (int64_t)j * fx + i;
+                const bool in = i <= f.nx && j <= f.ny && k <= f.nz && ANL_IN_RANGE(nf, fxy * (f.nz + 1));
+                const int64_t n = in ? nf : 0;
                 mv[g][bb][a] = in ? __ldg(nmf + n) : uint8_t(0);
 #pragma unroll
                 for (int e = 0; e < 3; ++e) xv[g][bb][a][e] = in ? xf[3 * n + e] : T(0);
@@ -1869,5 +1875,7 @@ int solver_dot(anl_ctx* c, const double* a, const double* b, double* out, cudaSt
     *out = c->red_h[0];
     return ANL_OK;
 }
+
+ANL_DEBUG_UNIT(solver)
 
 }  // namespace anl

@@ -339,6 +339,7 @@ struct TailCtx {
             const float* hi = ainv_hi + (int64_t)row * n;
             const float* lo = ainv_lo + (int64_t)row * n;
             for (int c = lane; c < n; c += 32) {
+                if (!ANL_IN_RANGE((int64_t)row * n + c, (int64_t)n * n)) break;
                 const float bc = b[c];
                 acc.add_prod(__ldg(hi + c), bc);
                 acc.add_prod(__ldg(lo + c), bc);
@@ -461,5 +462,7 @@ int launch_ainv_split(const double* ainv, int n, float* hi, float* lo, cudaStrea
     ANL_LAUNCH_CHECK();
     return ANL_OK;
 }
+
+ANL_DEBUG_UNIT(vtail)
 
 }  // namespace anl

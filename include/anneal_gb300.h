@@ -306,6 +306,12 @@ int anl_mg_info(anl_ctx* ctx, int* nlev_h, int* dims_h, double* lmax_h);
    the reference; lets a benchmark count the GPU launches inside its timed region). */
 int64_t anl_launch_count(void);
 
+/* Debug build only (no counterpart in the reference; the library built with -DANL_DEBUG=1):
+   the number of global-memory accesses the kernels' bounds checks caught and skipped since
+   the last call, and first_h[0..2] = index, extent and source line of the first; both
+   records are cleared. Synchronises the device. The normal build sets *count_h = -1. */
+int anl_debug_oob(long long* count_h, long long* first_h);
+
 /* Benchmark hook (no counterpart in the reference): launches the level-0 K u kernel
    `reps` times on `stream` between two CUDA events and writes the mean time per launch in
    milliseconds to *ms_h. The element scales are those of the last anl_apply_K / anl_solve

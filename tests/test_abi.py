@@ -48,3 +48,22 @@ def test_bad_arguments_are_rejected_before_any_device_work(lib_path):
     assert st == N.ANL_ERR_BADARG
     assert "bad arguments" in N.last_error()
     assert lib.anl_apply_K(None, None, None, None, None) == N.ANL_ERR_BADARG
+
+
+def test_release_build_has_no_bounds_checks(lib_path):
+    from anneal_gb300 import _native as N
+    if N.DEBUG_LIB:
+        pytest.skip("the debug library is loaded")
+    lib = N.load()
+    count, first = ctypes.c_longlong(0), (ctypes.c_longlong * 3)()
+    assert lib.anl_debug_oob(ctypes.byref(count), first) == N.ANL_OK
+    assert count.value == -1 and list(first) == [0, 0, 0]
+
+
+def test_debug_build_compiles_and_exports_every_declared_symbol():
+    from anneal_gb300 import build
+    path = build.build(debug=True)
+    assert path.endswith(os.path.join("_lib_debug", "libanneal_gb300.so"))
+    lib = ctypes.CDLL(path)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing

@@ -2,6 +2,8 @@
 
 Tolerances: FP64 paths agree to ~1e-12 relative; FP32 paths to a few 1e-6 of the field's
 largest magnitude (FP32 arithmetic with FP64 accumulation where the kernel reduces)."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -193,3 +195,15 @@ def test_stress_and_von_mises_match_reference(golden):
     sn = fem.normal_stress(sig, (0.2, -0.3, 1.0))
     assert np.abs(sn - g["sn"]).max() <= 1e-10 * np.abs(g["sn"]).max()
     fem.close()
+
+
+def test_bounds_checks_match_the_loaded_library():
+    """The bounds-checked build (ANL_DEBUG_LIB=1) reports a count (0 here: the tests before
+    it are checked by the conftest fixture); the normal build reports -1 (no checks)."""
+    import ctypes
+    from anneal_gb300 import _native as N
+    lib = N.load()
+    count, first = ctypes.c_longlong(0), (ctypes.c_longlong * 3)()
+    N.check(lib.anl_debug_oob(ctypes.byref(count), first), "anl_debug_oob")
+    assert N.LIB_PATH.endswith(os.path.join("_lib_debug" if N.DEBUG_LIB else "_lib", "libanneal_gb300.so"))
+    assert count.value == (0 if N.DEBUG_LIB else -1)
