@@ -207,8 +207,8 @@ static inline dim3 transfer_grid(const Dims& d, int nrhs = 1) {
 // issued before any is stored: read straight from the interleaved layout, the stride-2 node
 // pattern of a warp touched six times the sectors it used (3.9-6.6 us on the coarse levels
 // against 6.0-7.2 us before, the same 20-21 us on the finest). The same staging for the
-// prolongation's read-modify-write of the fine nodes was slower (66 against 38 us) and is
-// not used.
+// prolongation's read-modify-write of the fine nodes was slower (66 against 38 us at 12.8M
+// DOF, 25 us now that the prolongation issues all its loads first) and is not used.
 constexpr int TRF_X = 2 * TR_X + 1, TRF_Y = 2 * TR_Y + 1;  // fine nodes around a coarse tile
 
 // b_c = R r_f = P^T r_f (trilinear weights 1, 1/2, 1/4, 1/8), zero on fixed coarse DOFs. The
@@ -294,7 +294,8 @@ __global__ void __launch_bounds__(TR_X * TR_Y) k_restrict(Dims f, Dims c, const 
 // a, b, g in {0, 1}, from the up to 8 coarse nodes (I + a', J + b', K + g'). Every load of a
 // thread (coarse values, fine masks and fine values) is issued before the first store and
 // none depends on another, so one memory latency covers all of them (with the fine loads
-// behind a test of their mask, each fine node cost two latencies in turn: 38 us at 12.8M DOF).
+// behind a test of their mask, each fine node cost two latencies in turn: 38 us at 12.8M DOF
+// against 25 us).
 template <class T>
 __global__ void __launch_bounds__(TR_X * TR_Y, 4) k_prolong_add(Dims f, Dims c, const T* __restrict__ xc,
                                                                 const uint8_t* __restrict__ nmf, T* __restrict__ xf,
