@@ -46,7 +46,9 @@ struct KuArgs {
     const T* u = nullptr;            // input vector (masked: zeros on non-free DOFs)
     T* y = nullptr;                  // APPLY*: K u; RESID: b - K u
     const T* b = nullptr;            // RESID, CHEB
-    T* dv = nullptr;                 // CHEB: Chebyshev direction, updated in place
+    T* dv = nullptr;                 // CHEB: Chebyshev direction, updated in place; component-major
+                                     // (dv[c * N_n + n]): private to a sweep, so every warp store
+                                     // and load of it covers whole 32-byte sectors
     T* xout = nullptr;               // CHEB: u + new direction
     T c1 = T(0), c2 = T(0);          // CHEB: d <- c1 d + c2 D^-1 (b - K u)
     const double* cheb = nullptr;    // CHEB: {c1, c2} in device memory (overrides c1, c2)

@@ -268,7 +268,7 @@ struct KuTile {
             if (MODE == KU_CHEB) {
                 e.dg = __ldg(a.diag + n);
 #pragma unroll
-                for (int c = 0; c < 3; ++c) e.dv[c] = a.c1_zero ? T(0) : a.dv[3 * n + c];
+                for (int c = 0; c < 3; ++c) e.dv[c] = a.c1_zero ? T(0) : a.dv[c * plane * NZn + n];
             }
         }
     }
@@ -377,7 +377,7 @@ struct KuTile {
                 // plane in CHEB0, loaded with the epilogue inputs in CHEB
                 const T inv = T(MODE == KU_CHEB0 ? in.dg : ep.dg);
                 const T c1 = c1s, c2 = c2s;
-                T* dp = a.dv + 3 * n;
+                T* dp = a.dv + n;  // component-major: dp[c * N_n]
                 T* xp = a.xout + 3 * n;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -387,7 +387,7 @@ struct KuTile {
                         dn = c1 * dprev + c2 * (b[c] - y[c]) * inv;
                         xn = u[c] + dn;
                     }
-                    if (a.dv_keep) dp[c] = dn;
+                    if (a.dv_keep) dp[c * plane * NZn] = dn;
                     xp[c] = xn;
                 }
             }

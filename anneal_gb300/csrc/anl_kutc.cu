@@ -451,7 +451,8 @@ __global__ void __launch_bounds__(NT, 1) kutc_kernel(KuArgs<float> a, KeModal<fl
                                 const float inv = a.diag[n];
                                 const float c1 = a.cheb ? (float)a.cheb[0] : a.c1, c2 = a.cheb ? (float)a.cheb[1] : a.c2;
                                 const float c20 = MODE == KU_CHEB0 ? (float)a.cheb0[1] : 0.f;
-                                float* dp = a.dv + 3 * n;
+                                float* dp = a.dv + n;  // component-major: dp[c * N_n]
+                                const int64_t nnode = a.d.nn();
                                 float* xp = a.xout + 3 * n;
 #pragma unroll
                                 for (int c = 0; c < 3; ++c) {
@@ -461,11 +462,11 @@ __global__ void __launch_bounds__(NT, 1) kutc_kernel(KuArgs<float> a, KeModal<fl
                                         // the iterate: x1 = c2_0 D^-1 b (which is also the first
                                         // direction) in the fused pass, else the staged field
                                         const float uc = MODE == KU_CHEB0 ? c20 * inv * bc : __ldg(a.u + 3 * n + c);
-                                        const float dprev = MODE == KU_CHEB0 ? uc : (a.c1_zero ? 0.f : dp[c]);
+                                        const float dprev = MODE == KU_CHEB0 ? uc : (a.c1_zero ? 0.f : dp[c * nnode]);
                                         dn = c1 * dprev + c2 * (bc - y[c]) * inv;
                                         xn = uc + dn;
                                     }
-                                    if (a.dv_keep) dp[c] = dn;
+                                    if (a.dv_keep) dp[c * nnode] = dn;
                                     xp[c] = xn;
                                 }
                             }
