@@ -1,5 +1,5 @@
 """The CPU oracle against the golden fixtures generated by running the reference
-(tests/golden/make_golden.py). These pin the oracle before it judges the GPU path."""
+(tests/golden/make_golden.py). These pin the oracle before it checks the GPU path."""
 import json
 import os
 
