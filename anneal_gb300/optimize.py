@@ -58,6 +58,23 @@ def _continuation(it, iters, p_final, warm):
     return p_final if warm else min(p_final, 1.0 + 0.25 * ((it - 1) // hold))
 
 
+def galerkin_coefficients(g11, g12, g22, r1, r2):
+    """(a, b) minimising the energy x.Kx/2 - F.x of x = a u1 + b d over the two directions, from
+    g11 = u1.Ku1, g12 = u1.Kd, g22 = d.Kd, r1 = F.u1 and r2 = F.d; None where the start should
+    stay u1: a non-finite or degenerate matrix (d too small or too close to u1's direction
+    for FP32 entries to resolve), or a combination whose energy is not below u1's."""
+    if not all(np.isfinite(v) for v in (g11, g12, g22, r1, r2)) or not (g11 > 0 and g22 > 1e-12 * g11):
+        return None
+    det = g11 * g22 - g12 * g12
+    if not det > 1e-4 * g11 * g22:  # the FP32 entries resolve the two directions
+        return None
+    a, b = (r1 * g22 - r2 * g12) / det, (g11 * r2 - g12 * r1) / det
+    # Pi(x0) = -(a r1 + b r2) / 2 against Pi(u1) = g11 / 2 - r1
+    if not (np.isfinite(a) and np.isfinite(b) and -0.5 * (a * r1 + b * r2) <= 0.5 * g11 - r1):
+        return None
+    return a, b
+
+
 class SimpRunner:
     """The device-resident state of one SIMP run and one ``step()`` per iteration.
 
@@ -153,14 +170,7 @@ class SimpRunner:
         ctx, fem = self.ctx, self.fem
         self.it += 1
         it = self.it
-        p = self.p = _continuation(it, self.iters, self.p_final, self.warm)
-        if p >= self.p_final and not self.warm and self.beta_max > 0:   # optimize.py:111-116
-            if self.beta == 0:
-                self.beta, self.beta_since = 1.0, 0
-            elif self.beta_since >= self.beta_step and self.beta < self.beta_max:
-                self.beta, self.beta_since = min(self.beta_max, 2 * self.beta), 0
-            self.beta_since += 1
-        beta = self.beta
+        p, beta = self._advance_continuation(it)
         ctx.physical(self.x_t, self.frz_t, beta, ETA, self.xphys_t, self.dxp_t)
         ctx.stiffness_scale(self.xphys_t, self.phi_t, self.E0, self.emin, p, self.escale_t)
         last = fem.cg_iters[-1] if fem.cg_iters else None
@@ -213,6 +223,19 @@ class SimpRunner:
                  f"{rec['seconds']:.1f}s")
         return rec
 
+    def _advance_continuation(self, it):
+        """Penalty and projection sharpness of iteration `it` (optimize.py:105-116): p from the
+        ramp, beta from 1 once p is final, doubled every beta_step iterations up to beta_max.
+        Advances the beta state; returns (p, beta)."""
+        p = self.p = _continuation(it, self.iters, self.p_final, self.warm)
+        if p >= self.p_final and not self.warm and self.beta_max > 0:   # optimize.py:111-116
+            if self.beta == 0:
+                self.beta, self.beta_since = 1.0, 0
+            elif self.beta_since >= self.beta_step and self.beta < self.beta_max:
+                self.beta, self.beta_since = min(self.beta_max, 2 * self.beta), 0
+            self.beta_since += 1
+        return p, self.beta
+
     def _history_start(self):
         """CG start from the last two solutions. The reference starts each solve from the
         previous solution u1 (optimize.py:122); here the start is the energy-optimal
@@ -256,15 +279,7 @@ class SimpRunner:
         v = vals.cpu().numpy().astype(np.float64)
         for c in range(nc):
             g11, g12, g22 = v[c]
-            r1, r2 = float(c1[c]), float(c1[c]) - float(c2[c])
-            coef = None
-            if np.all(np.isfinite(v[c])) and g11 > 0 and g22 > 1e-12 * g11:
-                det = g11 * g22 - g12 * g12
-                if det > 1e-4 * g11 * g22:  # the FP32 entries resolve the two directions
-                    a, b = (r1 * g22 - r2 * g12) / det, (g11 * r2 - g12 * r1) / det
-                    # Pi(x0) = -(a r1 + b r2) / 2 against Pi(u1) = g11 / 2 - r1
-                    if np.isfinite(a) and np.isfinite(b) and -0.5 * (a * r1 + b * r2) <= 0.5 * g11 - r1:
-                        coef = (a, b)
+            coef = galerkin_coefficients(g11, g12, g22, float(c1[c]), float(c1[c]) - float(c2[c]))
             if coef is None:
                 U2[c].copy_(U1[c])
             else:   # x0 = (a + b) u1 - b u2, into the older solution's storage

@@ -1,0 +1,85 @@
+"""Host-side logic on the CPU: the continuation schedule against the reference's recorded runs,
+the CG start's Galerkin rule, the synthetic workloads' sizes and the benchmark's byte counts."""
+import numpy as np
+import pytest
+
+from anneal_gb300 import optimize as O
+from anneal_gb300 import problems as P
+
+
+def _schedule(iters, warm, beta_max, n, p_final=3.0):
+    """(p, beta) of SIMP iterations 1..n through SimpRunner's own state machine."""
+    r = O.SimpRunner.__new__(O.SimpRunner)
+    r.iters, r.p_final, r.warm, r.beta_max = iters, p_final, warm, beta_max
+    r.beta = beta_max / 2 if warm else 0.0
+    r.beta_since = 0
+    r.beta_step = max(5, int(0.12 * iters))
+    out = [r._advance_continuation(it) for it in range(1, n + 1)]
+    return np.array([p for p, _ in out]), np.array([b for _, b in out])
+
+
+@pytest.mark.parametrize("name, warm, beta_max", [
+    ("simp_small.npz", False, O.BETA_MAX),        # penalty ramp, then projection continuation
+    ("simp_small_tight.npz", False, O.BETA_MAX),
+    ("simp_worst.npz", True, O.BETA_MAX),         # warm start: p final, beta_max / 2 throughout
+    ("simp_config1.npz", True, 0.0),              # warm start without projection
+])
+def test_continuation_matches_the_reference_history(golden, name, warm, beta_max):
+    """optimize.py:105-116: the p and beta of every iteration of the reference's own runs."""
+    g = golden(name)
+    n = len(g["h_p"])
+    p, beta = _schedule(int(g["iters"]), warm, beta_max, n)
+    assert np.array_equal(p, g["h_p"])
+    assert np.array_equal(beta, g["h_beta"])
+
+
+def test_galerkin_coefficients_minimise_the_energy():
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        A = rng.normal(size=(2, 2))
+        G = A @ A.T + 0.05 * np.eye(2)
+        r = rng.normal(size=2)
+        c = O.galerkin_coefficients(G[0, 0], G[0, 1], G[1, 1], r[0], r[1])
+        pi_u1 = 0.5 * G[0, 0] - r[0]
+        best = np.linalg.solve(G, r)
+        if -0.5 * best @ r <= pi_u1 and np.linalg.det(G) > 1e-4 * G[0, 0] * G[1, 1]:
+            assert c is not None and np.allclose(c, best, rtol=1e-10, atol=1e-12)
+            assert -0.5 * np.dot(c, r) <= pi_u1 + 1e-12
+    # the start stays u1 where the two directions cannot be resolved or a value is not finite
+    assert O.galerkin_coefficients(1.0, 0.0, 1e-13, 1.0, 0.0) is None
+    assert O.galerkin_coefficients(1.0, 0.99999, 1.0, 1.0, 1.0) is None
+    assert O.galerkin_coefficients(1.0, 0.0, 1.0, float("nan"), 0.0) is None
+    assert O.galerkin_coefficients(-1.0, 0.0, 1.0, 1.0, 0.0) is None
+    # d orthogonal to u1 in the K inner product: each direction takes its own projection
+    assert np.allclose(O.galerkin_coefficients(2.0, 0.0, 4.0, 1.0, 2.0), (0.5, 0.5))
+
+
+def test_workloads_have_the_stated_sizes():
+    """The configurations' sizes: 48x24x24 cantilever (27,648 elements, 91,875 DOF), the
+    192x96x96 L-bracket (1,327,104 of 1,769,472 elements active, 5,447,811 DOF), the same at
+    256x128x128 (3,145,728 of 4,194,304, 12,830,211 DOF), the six-case bracket at 160x80x80
+    (1,024,000 elements, 3,168,963 DOF, six load cases)."""
+    c = P.cantilever()
+    assert c.shape == (48, 24, 24) and c.nelem == 27648 and c.ndof == 91875
+    for scale, shape, act, dof in ((1.0, (192, 96, 96), 1327104, 5447811),
+                                   (4 / 3, (256, 128, 128), 3145728, 12830211)):
+        w = P.lbracket(scale=scale)
+        assert w.shape == shape and int(np.asarray(w.active).sum()) == act and w.ndof == dof
+        assert len(w.loads) == 1
+        F = next(iter(w.loads.values()))
+        assert abs(F.sum() + 1.0) < 1e-12 and np.all(F[0::3] == 0) and np.all(F[1::3] == 0)
+    s = P.six_case_bracket()
+    assert s.shape == (160, 80, 80) and s.nelem == 1024000 and s.ndof == 3168963 and len(s.loads) == 6
+
+
+def test_bench_byte_counts():
+    """The benchmark's algorithmic bytes per finest-level pass at 256x128x128: K u is
+    24 N_n + 4 N_e = 119.4 MB (u and y as FP32 nodes, E as FP32 elements)."""
+    import bench
+    nn, ne = 257 * 129 * 129, 256 * 128 * 128
+    by = {name: f(nn, ne) for _, name, _, f in bench.PASSES}
+    assert by["K u"] == 24 * nn + 4 * ne and abs(by["K u"] / 1e6 - 119.4) < 0.05
+    assert by["residual b - K x"] == 36 * nn + 4 * ne
+    assert by["last Chebyshev step of a sweep"] == by["first Chebyshev step after the prolongation"] == 52 * nn + 4 * ne
+    assert by["first two Chebyshev steps"] == 28 * nn + 4 * ne
+    assert bench.KU_DENSE_FLOPS == 1152
