@@ -1,5 +1,7 @@
 """Host-side logic on the CPU: the continuation schedule against the reference's recorded runs,
-the CG start's Galerkin rule, the synthetic workloads' sizes and the benchmark's byte counts."""
+the CG start's Galerkin rule, the synthetic workloads' sizes, the benchmark's byte counts, the
+element matrices against the reference's golden values and the grid against the reference's
+own Grid (where its source tree is present)."""
 import numpy as np
 import pytest
 
@@ -83,3 +85,47 @@ def test_bench_byte_counts():
     assert by["last Chebyshev step of a sweep"] == by["first Chebyshev step after the prolongation"] == 52 * nn + 4 * ne
     assert by["first two Chebyshev steps"] == 28 * nn + 4 * ne
     assert bench.KU_DENSE_FLOPS == 1152
+
+
+def test_hex8_matrices_match_the_reference_golden(golden):
+    """fem.py:71-84: Ke, B0 and D of the reference for three (nu, h)."""
+    from anneal_gb300 import fem
+    g = golden("ke.npz")
+    for t in "abc":
+        ke, B0, D = fem.hex8_matrices(float(g[f"nu_{t}"]), float(g[f"h_{t}"]))
+        for got, key in ((ke, "ke"), (B0, "B0"), (D, "D")):
+            want = g[f"{key}_{t}"]
+            assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max(), (key, t)
+
+
+REF = "/root/reference"
+
+
+@pytest.mark.skipif(not __import__("os").path.isfile(REF + "/anneal/fem.py"),
+                    reason="reference tree not present on this machine")
+def test_grid_matches_the_reference_grid():
+    """fem.py:87-127: element nodes, node coordinates, element centres and the flat <-> [i, j, k]
+    maps of the reference's own Grid, on a ragged grid with an offset origin."""
+    import os
+    import sys
+    from anneal_gb300 import fem
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    saved = {k: sys.modules[k] for k in list(sys.modules) if k == "anneal" or k.startswith("anneal.")
+             or k in ("pyamg", "trimesh")}
+    try:
+        import make_golden
+        rfem, _, _ = make_golden.install_stubs(REF)
+        shape, h, origin = (7, 5, 4), 0.37, (1.5, -2.0, 0.25)
+        a, b = fem.Grid(shape, h, origin), rfem.Grid(shape, h, origin)
+        assert (a.nelem, a.nnode, a.shape) == (b.nelem, b.nnode, b.shape)
+        e = np.arange(a.nelem)
+        n = np.arange(a.nnode)
+        assert np.array_equal(a.element_nodes(e), b.element_nodes(e))
+        assert np.array_equal(a.node_coords(n), b.node_coords(n))
+        assert np.array_equal(a.elem_centers(), b.elem_centers())
+        f = np.random.default_rng(0).random(a.nelem)
+        assert np.array_equal(a.to3d(f), b.to3d(f)) and np.array_equal(a.to1d(a.to3d(f)), f)
+    finally:
+        for k in [k for k in sys.modules if k == "anneal" or k.startswith("anneal.") or k in ("pyamg", "trimesh")]:
+            del sys.modules[k]
+        sys.modules.update(saved)
