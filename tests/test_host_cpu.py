@@ -129,3 +129,16 @@ def test_grid_matches_the_reference_grid():
         for k in [k for k in sys.modules if k == "anneal" or k.startswith("anneal.") or k in ("pyamg", "trimesh")]:
             del sys.modules[k]
         sys.modules.update(saved)
+
+
+def test_many_part_set_is_seeded_and_in_range():
+    """The many-part set: 32 seeded cantilevers, nx in [32, 128], ny and nz in [16, 64], volume
+    fraction in [0.2, 0.4], filter radius in [1.2, 2.5]; 16.0M DOF in total for seed 0."""
+    from anneal_gb300 import batch as B
+    a, b = B.seeded_parts(32, 0), B.seeded_parts(32, 0)
+    assert [p.shape for p in a] == [p.shape for p in b]
+    for p in a:
+        nx, ny, nz = p.shape
+        assert 32 <= nx <= 128 and 16 <= ny <= 64 and 16 <= nz <= 64
+        assert 0.2 <= p.vf <= 0.4 and 1.2 <= p.r_vox <= 2.5
+    assert abs(sum(p.ndof for p in a) / 1e6 - 16.0) < 0.05
